@@ -1,0 +1,305 @@
+"""disccofan_gb300 -- GB300 component-forest hot path behind a C ABI.
+
+Python view of ``libdcf_gb300.so`` (declared in ``include/dcf.h``).  It mirrors the
+reference's operator surface for this path -- tree type, connectivity, attribute
+index, lambda, filter rule, lambda-vector bins -- with the reference's names:
+
+    ctx  = Context()
+    tree = ctx.build(image, connectivity=4, tree_type="max", attribute=0)
+    out  = tree.filter(attribute=0, lam=200.0, rule="direct")      # tree_filtering
+    chk  = tree.check(attribute=0)                                 # tree_attribute_check
+    spec = tree.pattern_spectrum(0, lvec)                          # tree_pattern_spectrum
+    spec = tree.pattern_spectrum2d(14, lvec1, 0, lvec2)            # tree_pattern_spectrum2d
+
+Images are numpy arrays (host memory) or CUDA torch tensors (device memory, used in
+place).  Every computation runs in the CUDA library; there is no CPU fallback, and
+importing this module fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdcf_gb300.so")
+
+DTYPES = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1, np.dtype(np.uint32): 2, np.dtype(np.float32): 3}
+RULES = {"direct": 0, "min": 1, "max": 2, "subtractive": 3}
+TREE_TYPES = {"max": 0, "min": 1}
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "device loop bound exceeded",
+          5: "image contains NaN", 6: "invalid state", 7: "I/O error", 8: "unsupported"}
+
+# attribute names, in the reference's AttribsArray order (attributes.c:1224-1248) + 18
+ATTRIBUTES = ["area", "rectarea", "rectdiag", "xext", "yext", "zext", "xmean", "ymean", "zmean", "xwmean",
+              "ywmean", "zwmean", "flux", "inertiatrace", "elong", "flat", "spars", "ncomp", "bboxelong"]
+ATTR_GROUP = [0, 1, 1, 1, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4, 1]
+
+
+class DcfError(RuntimeError):
+    def __init__(self, status: int, detail: str = ""):
+        self.status = status
+        super().__init__(f"dcf: {STATUS.get(status, status)}" + (f" ({detail})" if detail else ""))
+
+
+class _Image(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("dtype", C.c_int), ("on_device", C.c_int), ("dims", C.c_uint64 * 3),
+                ("connectivity", C.c_int), ("tree_type", C.c_int), ("pixdim", C.c_float * 3)]
+
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """Load libdcf_gb300.so (raises if it was not built: no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(LIB_PATH)
+    vp, i, d, u64 = C.c_void_p, C.c_int, C.c_double, C.c_uint64
+    sig = {
+        "dcf_ctx_create": [i, vp, C.POINTER(vp)],
+        "dcf_ctx_destroy": [vp],
+        "dcf_ctx_synchronize": [vp],
+        "dcf_tree_build": [vp, C.POINTER(_Image), i, C.POINTER(vp)],
+        "dcf_tree_set_attribute": [vp, vp, i],
+        "dcf_tree_destroy": [vp],
+        "dcf_tree_info": [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(i), C.POINTER(C.c_float)],
+        "dcf_tree_parent": [vp, vp, vp, i],
+        "dcf_tree_gval": [vp, vp, vp, i],
+        "dcf_node_attribute": [vp, vp, i, i, vp, i],
+        "dcf_filter": [vp, vp, i, i, d, i, vp, i],
+        "dcf_attribute_check": [vp, vp, i, vp, i],
+        "dcf_dmp": [vp, vp, i, i, vp, i, vp, i],
+        "dcf_pattern_spectrum": [vp, vp, i, vp, i, vp, i],
+        "dcf_pattern_spectrum2d": [vp, vp, i, vp, i, i, vp, i, vp, i],
+        "dcf_lvec_read": [C.c_char_p, d, vp, i, C.POINTER(i)],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    L.dcf_ctx_last_error.argtypes = [vp]
+    L.dcf_ctx_last_error.restype = C.c_char_p
+    L.dcf_status_string.argtypes = [C.c_int]
+    L.dcf_status_string.restype = C.c_char_p
+    L.dcf_ctx_launch_count.argtypes = [vp]
+    L.dcf_ctx_launch_count.restype = C.c_uint64
+    _lib = L
+    return L
+
+
+def _is_torch_cuda(x) -> bool:
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+def lvec_from_values(values, imscale: float = 1.0) -> np.ndarray:
+    """The bins lambda_vector_read builds from file values: [0, v1/imscale, ...] (float32)."""
+    out = [np.float32(0.0)]
+    for v in values:
+        out.append(np.float32(np.float64(np.float32(v)) / imscale))
+    return np.array(out, dtype=np.float32)
+
+
+def read_lvec(path: str, imscale: float = 1.0) -> np.ndarray:
+    """Read a "#LambdaVector file..." file exactly as the reference does (lambdavec.c:35)."""
+    L = library()
+    n = C.c_int(0)
+    st = L.dcf_lvec_read(path.encode(), imscale, None, 0, C.byref(n))
+    if st:
+        raise DcfError(st, path)
+    out = np.empty(n.value, np.float32)
+    st = L.dcf_lvec_read(path.encode(), imscale, out.ctypes.data, out.size, C.byref(n))
+    if st:
+        raise DcfError(st, path)
+    return out
+
+
+class Context:
+    """One GPU, one CUDA stream, reusable device workspace (dcf_ctx)."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self.lib = library()
+        h = C.c_void_p()
+        st = self.lib.dcf_ctx_create(device, C.c_void_p(stream) if stream else None, C.byref(h))
+        if st:
+            raise DcfError(st, "dcf_ctx_create")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dcf_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st: int, what: str = ""):
+        if st:
+            detail = self.lib.dcf_ctx_last_error(self.h).decode(errors="replace")
+            raise DcfError(st, f"{what}: {detail}" if what else detail)
+
+    def synchronize(self):
+        self.check(self.lib.dcf_ctx_synchronize(self.h), "synchronize")
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.dcf_ctx_launch_count(self.h))
+
+    def build(self, image, connectivity: int = 4, tree_type: str = "max", attribute: int = 0,
+              pixdim=(1.0, 1.0, 1.0)) -> "Tree":
+        """build_tree_with_attributes: tree of a 2-D (H, W) or 3-D (D, H, W) image."""
+        return Tree(self, image, connectivity, tree_type, attribute, pixdim)
+
+
+class Tree:
+    def __init__(self, ctx: Context, image, connectivity, tree_type, attribute, pixdim):
+        self.ctx = ctx
+        L = ctx.lib
+        on_dev = _is_torch_cuda(image)
+        if on_dev:
+            import torch
+            tdt = {torch.uint8: np.uint8, torch.uint16: np.uint16, torch.int32: None,
+                   torch.float32: np.float32}.get(image.dtype)
+            if image.dtype == getattr(torch, "uint32", None):
+                tdt = np.uint32
+            if tdt is None:
+                raise TypeError(f"unsupported tensor dtype {image.dtype}")
+            if not image.is_contiguous():
+                raise ValueError("device image must be contiguous")
+            dt = np.dtype(tdt)
+            ptr = image.data_ptr()
+            shape = tuple(image.shape)
+            self._keep = image
+        else:
+            arr = np.ascontiguousarray(image)
+            if arr.dtype not in DTYPES:
+                raise TypeError(f"unsupported image dtype {arr.dtype} (u8, u16, u32, f32)")
+            dt = arr.dtype
+            ptr = arr.ctypes.data
+            shape = arr.shape
+            self._keep = arr
+        if len(shape) == 2:
+            d, h, w = 1, shape[0], shape[1]
+        elif len(shape) == 3:
+            d, h, w = shape
+        else:
+            raise ValueError("image must be 2-D or 3-D")
+        self.shape = tuple(shape)
+        im = _Image(ptr, DTYPES[dt], int(on_dev), (C.c_uint64 * 3)(w, h, d), connectivity,
+                    TREE_TYPES[tree_type], (C.c_float * 3)(*pixdim))
+        hnd = C.c_void_p()
+        ctx.check(L.dcf_tree_build(ctx.h, C.byref(im), attribute, C.byref(hnd)), "dcf_tree_build")
+        self.h = hnd
+        self.n = w * h * d
+        self.attribute = attribute
+        self.tree_type = tree_type
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.dcf_tree_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- helpers -----------------------------------------------------------
+    def _out(self, dtype, out=None, count=None):
+        count = self.n if count is None else count
+        if out is not None:
+            if _is_torch_cuda(out):
+                return out, out.data_ptr(), 1
+            return out, out.ctypes.data, 0
+        a = np.empty(count, dtype)
+        return a, a.ctypes.data, 0
+
+    def _shape(self, a, lead=()):
+        return a.reshape(lead + self.shape) if isinstance(a, np.ndarray) else a
+
+    def set_attribute(self, attribute: int):
+        """flood_attributes: accumulate a new attribute group on this tree."""
+        self.ctx.check(self.ctx.lib.dcf_tree_set_attribute(self.ctx.h, self.h, attribute), "set_attribute")
+        self.attribute = attribute
+
+    def _ensure_group(self, attribute: int):
+        if ATTR_GROUP[attribute] != ATTR_GROUP[self.attribute]:
+            self.set_attribute(attribute)
+
+    def info(self):
+        n, m, c, g = C.c_uint64(), C.c_uint64(), C.c_int(), C.c_float()
+        self.ctx.check(self.ctx.lib.dcf_tree_info(self.h, C.byref(n), C.byref(m), C.byref(c), C.byref(g)), "info")
+        return {"pixels": n.value, "nodes": m.value, "connectivity": c.value, "max_gval": g.value}
+
+    # -- tree data ---------------------------------------------------------
+    def parent(self, out=None):
+        a, p, dev = self._out(np.int64, out)
+        self.ctx.check(self.ctx.lib.dcf_tree_parent(self.ctx.h, self.h, p, dev), "parent")
+        return a
+
+    def gval(self, out=None):
+        a, p, dev = self._out(np.float32, out)
+        self.ctx.check(self.ctx.lib.dcf_tree_gval(self.ctx.h, self.h, p, dev), "gval")
+        return a
+
+    def node_attribute(self, attribute: int, area: bool = False, out=None):
+        self._ensure_group(attribute)
+        a, p, dev = self._out(np.float64, out)
+        self.ctx.check(self.ctx.lib.dcf_node_attribute(self.ctx.h, self.h, attribute, int(area), p, dev),
+                       "node_attribute")
+        return a
+
+    # -- operations (operation.c) ------------------------------------------
+    def filter(self, attribute: int, lam: float, rule="direct", extract: bool = False, out=None):
+        self._ensure_group(attribute)
+        r = RULES[rule] if isinstance(rule, str) else int(rule)
+        a, p, dev = self._out(np.float32, out)
+        self.ctx.check(self.ctx.lib.dcf_filter(self.ctx.h, self.h, attribute, r, float(lam), int(extract), p, dev),
+                       "filter")
+        return self._shape(a)
+
+    def check(self, attribute: int, out=None):
+        self._ensure_group(attribute)
+        a, p, dev = self._out(np.float32, out)
+        self.ctx.check(self.ctx.lib.dcf_attribute_check(self.ctx.h, self.h, attribute, p, dev), "check")
+        return self._shape(a)
+
+    def dmp(self, attribute: int, lvec, rule="direct", out=None):
+        self._ensure_group(attribute)
+        lv = np.ascontiguousarray(lvec, np.float32)
+        r = RULES[rule] if isinstance(rule, str) else int(rule)
+        a, p, dev = self._out(np.float32, out, count=(lv.size - 1) * self.n)
+        self.ctx.check(self.ctx.lib.dcf_dmp(self.ctx.h, self.h, attribute, r, lv.ctypes.data, lv.size, p, dev), "dmp")
+        return self._shape(a, (lv.size - 1,))
+
+    def pattern_spectrum(self, attribute: int, lvec, out=None):
+        """lvec: bins including the leading 0 (read_lvec / lvec_from_values)."""
+        self._ensure_group(attribute)
+        lv = np.ascontiguousarray(lvec, np.float32)
+        spec = out if out is not None else np.zeros(lv.size, np.float64)
+        dev = int(_is_torch_cuda(spec))
+        p = spec.data_ptr() if dev else spec.ctypes.data
+        self.ctx.check(self.ctx.lib.dcf_pattern_spectrum(self.ctx.h, self.h, attribute, lv.ctypes.data, lv.size, p,
+                                                         dev), "pattern_spectrum")
+        return spec
+
+    def pattern_spectrum2d(self, attr1: int, lvec1, attr2: int, lvec2, out=None):
+        """spectrum[s2, s1] (row-major [n2, n1]), the reference's s1 + s2*n1 layout."""
+        self._ensure_group(attr1)
+        l1 = np.ascontiguousarray(lvec1, np.float32)
+        l2 = np.ascontiguousarray(lvec2, np.float32)
+        spec = out if out is not None else np.zeros((l2.size, l1.size), np.float64)
+        dev = int(_is_torch_cuda(spec))
+        p = spec.data_ptr() if dev else spec.ctypes.data
+        self.ctx.check(self.ctx.lib.dcf_pattern_spectrum2d(self.ctx.h, self.h, attr1, l1.ctypes.data, l1.size, attr2,
+                                                           l2.ctypes.data, l2.size, p, dev), "pattern_spectrum2d")
+        return spec

@@ -1,0 +1,73 @@
+"""Build libdcf_gb300.so in-tree: nvcc for sm_103a, one -gencode, units compiled in
+parallel, then one shared-library link.  No cmake; re-run is incremental by mtime."""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libdcf_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+CU_UNITS = ["dcf_build.cu", "dcf_attr.cu", "dcf_ops.cu", "dcf_api.cu"]
+C_UNITS = ["dcf_host.c"]
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+NVFLAGS = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+           "-Xptxas", "-warn-spills", "-I" + CSRC, "-I" + INCLUDE]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _deps() -> float:
+    newest = 0.0
+    for d in (CSRC, INCLUDE):
+        for f in os.listdir(d):
+            newest = max(newest, os.path.getmtime(os.path.join(d, f)))
+    return newest
+
+
+def _compile(src: str, verbose: bool) -> str:
+    out = os.path.join(OBJ, src + ".o")
+    if os.path.exists(out) and os.path.getmtime(out) >= _deps():
+        return out
+    if src.endswith(".cu"):
+        cmd = [nvcc(), *NVFLAGS, "-c", os.path.join(CSRC, src), "-o", out]
+    else:
+        cmd = ["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", "-I" + INCLUDE, "-c", os.path.join(CSRC, src), "-o", out]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile of {src} failed:\n{r.stdout}\n{r.stderr}")
+    if verbose and r.stderr.strip():
+        print(r.stderr, flush=True)
+    return out
+
+
+def build(verbose: bool = False) -> str:
+    os.makedirs(OBJ, exist_ok=True)
+    units = CU_UNITS + C_UNITS
+    with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), units))
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
+        return LIB
+    cmd = [nvcc(), GENCODE, "-shared", "-o", LIB, *objs, "-lcudart"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

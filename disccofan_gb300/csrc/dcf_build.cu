@@ -1,0 +1,312 @@
+// Tree construction kernels (the reference's build_local_tree_generic,
+// flood.c:58-172, and its distributed correction, boundary.c:1712, re-designed for
+// one GPU):
+//
+//   k_stats        min / max / NaN scan of the input (preprocessing.c:7-30).
+//   k_tile_build   one CTA builds the max-tree of one tile in shared memory: a 1-D
+//                  stack pass per row, then the rows are merged band by band with the
+//                  lock-free connect() on 16-bit shared-memory parents; the tile's
+//                  forest is written to HBM in canonical (level-root) form.
+//   k_seam_merge   every edge that crosses a tile boundary is merged with connect()
+//                  on the int32 parent array in HBM (32-bit CAS): the on-device
+//                  replacement of the MPI boundary-tree exchange and merge.
+//   k_canon_*      flatten to the reference's canonical form (flood.c:127-141,
+//                  get_levelroot :693-712): pixel -> level root, root -> parent's root.
+#include "dcf_kernels.cuh"
+
+namespace dcf {
+
+// ---------------------------------------------------------------------------
+// statistics
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_stats(const T *__restrict__ img, long long n, unsigned *kmin, unsigned *kmax,
+                        unsigned *nan_count)
+{
+    unsigned lo = 0xFFFFFFFFu, hi = 0u, nans = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float v = to_float<T>(img[i]);
+        if (v != v) {
+            nans++;
+            continue;
+        }
+        unsigned k = order_key(v);
+        lo = min(lo, k);
+        hi = max(hi, k);
+    }
+    for (int o = 16; o; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        nans += __shfl_xor_sync(0xffffffffu, nans, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(kmin, lo);
+        atomicMax(kmax, hi);
+        if (nans) atomicAdd(nan_count, nans);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// tile build
+// ---------------------------------------------------------------------------
+constexpr unsigned short SNONE = 0xFFFFu;
+
+struct SmemAcc {
+    const uint32_t *k;
+    unsigned short *p;
+    unsigned *err;
+    __device__ uint32_t key(int i) const { return k[i]; }
+    __device__ long long walk_bound() const { return TILE_PIX + 1; }
+    __device__ int par(int i) const
+    {
+        unsigned short v = ((volatile unsigned short *)p)[i];
+        return v == SNONE ? NONE : (int)v;
+    }
+    __device__ void set_par(int i, int v) { ((volatile unsigned short *)p)[i] = (unsigned short)v; }
+    __device__ bool cas_par(int i, int expect, int v)
+    {
+        unsigned short e = expect == NONE ? SNONE : (unsigned short)expect;
+        return atomicCAS(p + i, e, (unsigned short)v) == e;
+    }
+    __device__ void error(unsigned bit) { raise_error(err, bit); }
+};
+
+template <typename T, bool MIN>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__restrict__ gval,
+             int *__restrict__ parent, unsigned *err)
+{
+    const float gmax = MIN ? key_to_level(*kmax) : 0.0f;
+    // tile extents: 2-D 64x64, 3-D 16x16x16 (4096 pixels, 16-bit local indices)
+    const bool is3d = g.D > 1;
+    const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
+    __shared__ uint32_t skey[TILE_PIX];
+    __shared__ unsigned short spar[TILE_PIX];
+    __shared__ unsigned short sstk[TILE_PIX];  // one TW-long stack per row
+
+    const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, z0 = blockIdx.z * TD;
+    const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
+    const int tid = threadIdx.x;
+
+    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
+        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
+        spar[i] = SNONE;
+        if (lx < wl && ly < hl && lz < dl) {
+            long long gp = (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
+            float lv = level_of<T, MIN>(img[gp], gmax);
+            gval[gp] = lv;
+            skey[i] = order_key(lv);
+        }
+    }
+    __syncthreads();
+
+    // 1-D max-tree of each row with a stack (pop higher keys; the popped chain
+    // hangs off the next popped element, the last one off the new pixel).
+    const int nrows = TH * TD;
+    for (int r = tid; r < nrows; r += TILE_THREADS) {
+        int ly = r % TH, lz = r / TH;
+        if (ly >= hl || lz >= dl) continue;
+        unsigned short *stk = sstk + r * TW;
+        int sp = 0;
+        const int base = r * TW;
+        for (int lx = 0; lx < wl; lx++) {
+            int i = base + lx;
+            uint32_t ki = skey[i];
+            int last = NONE;
+            while (sp > 0 && skey[stk[sp - 1]] > ki) {
+                int t = stk[--sp];
+                if (last != NONE) spar[last] = (unsigned short)t;
+                last = t;
+            }
+            if (last != NONE) spar[last] = (unsigned short)i;
+            stk[sp++] = (unsigned short)i;
+        }
+        for (int j = sp - 1; j >= 1; j--) spar[stk[j]] = stk[j - 1];
+    }
+    __syncthreads();
+
+    SmemAcc acc{skey, spar, err};
+    const Offs offs = forward_offsets(g.conn);
+    // merge row bands along y (each z slice), then slabs along z; at level k the
+    // seams are the rows (slices) c with c % 2^(k+1) == 2^k
+    for (int axis = 1; axis <= (is3d ? 2 : 1); axis++) {
+        const int ext = axis == 1 ? TH : TD;
+        for (int half = 1; half < ext; half <<= 1) {
+            const int nseams = (ext + 2 * half - 1) / (2 * half);
+            const int other = axis == 1 ? TD : TH;  // slices (axis y) or rows (axis z)
+            const long long work = (long long)nseams * other * TW;
+            for (long long w = tid; w < work; w += TILE_THREADS) {
+                int lx = (int)(w % TW);
+                long long rest = w / TW;
+                int o = (int)(rest % other);
+                int s = (int)(rest / other);
+                int c = s * 2 * half + half;  // seam coordinate on the axis
+                int ly, lz;
+                if (axis == 1) { ly = c; lz = o; }
+                else { lz = c; ly = o; }
+                if (lx >= wl || ly >= hl || lz >= dl) continue;
+                int p = lx + ly * TW + lz * TW * TH;
+                // edges from p to the previous row / slice: the reversed forward offsets
+                for (int e = 0; e < offs.n; e++) {
+                    int dx = offs.d[e][0], dy = offs.d[e][1], dz = offs.d[e][2];
+                    bool crosses = axis == 1 ? (dz == 0 && dy == 1) : (dz == 1);
+                    if (!crosses) continue;
+                    int qx = lx - dx, qy = ly - dy, qz = lz - dz;
+                    if (qx < 0 || qx >= wl || qy < 0 || qy >= hl || qz < 0 || qz >= dl) continue;
+                    if (axis == 2 && (qy < 0 || qy >= hl)) continue;
+                    connect(acc, p, qx + qy * TW + qz * TW * TH, MERGE_BOUND_SMEM);
+                }
+            }
+            __syncthreads();
+        }
+    }
+
+    // canonical form inside the tile: pixel -> level root, root -> parent's level root
+    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
+        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
+        if (lx >= wl || ly >= hl || lz >= dl) continue;
+        int r = levelroot(acc, i);
+        if (r != i) acc.set_par(i, r);
+    }
+    __syncthreads();
+    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
+        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
+        if (lx >= wl || ly >= hl || lz >= dl) continue;
+        int p = acc.par(i);
+        if (p != NONE && skey[p] < skey[i]) {  // level root: point at the parent's level root
+            int q = acc.par(p);
+            if (q != NONE && skey[q] == skey[p]) p = q;
+        }
+        int out;
+        if (p == NONE) {
+            out = NONE;
+        } else {
+            int px = p % TW, py = (p / TW) % TH, pz = p / (TW * TH);
+            out = (int)((long long)(z0 + pz) * g.WH + (long long)(y0 + py) * g.W + (x0 + px));
+        }
+        long long gp = (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
+        parent[gp] = out;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// seam merge in HBM
+// ---------------------------------------------------------------------------
+struct GlobalAcc {
+    const float *gv;
+    int *p;
+    unsigned *err;
+    long long n;
+    __device__ uint32_t key(int i) const { return order_key(gv[i]); }
+    __device__ long long walk_bound() const { return n + 1; }
+    __device__ int par(int i) const { return ((volatile int *)p)[i]; }
+    __device__ void set_par(int i, int v) { ((volatile int *)p)[i] = v; }
+    __device__ bool cas_par(int i, int expect, int v) { return atomicCAS(p + i, expect, v) == expect; }
+    __device__ void error(unsigned bit) { raise_error(err, bit); }
+};
+
+// One thread per pixel on a tile's shell; every forward edge that leaves the tile
+// is merged.  Each cross-tile edge has exactly one low endpoint, so none repeats.
+__global__ void k_seam_merge(const float *__restrict__ gval, Geom g, int *parent, unsigned *err)
+{
+    const bool is3d = g.D > 1;
+    const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
+    GlobalAcc acc{gval, parent, err, g.N};
+    const Offs offs = forward_offsets(g.conn);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
+         p += (long long)gridDim.x * blockDim.x) {
+        int x = (int)(p % g.W), y = (int)((p / g.W) % g.H), z = (int)(p / g.WH);
+        int lx = x % TW, ly = y % TH, lz = z % TD;
+        bool shell = lx == 0 || lx == TW - 1 || ly == 0 || ly == TH - 1 || (is3d && (lz == 0 || lz == TD - 1));
+        if (!shell) continue;
+        for (int e = 0; e < offs.n; e++) {
+            int qx = x + offs.d[e][0], qy = y + offs.d[e][1], qz = z + offs.d[e][2];
+            if (qx < 0 || qx >= g.W || qy < 0 || qy >= g.H || qz >= g.D) continue;
+            if (qx / TW == x / TW && qy / TH == y / TH && qz / TD == z / TD) continue;
+            int q = (int)((long long)qz * g.WH + (long long)qy * g.W + qx);
+            connect(acc, (int)p, q, MERGE_BOUND_GLOBAL);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// canonical form
+// ---------------------------------------------------------------------------
+__global__ void k_canon_pixels(const float *__restrict__ gval, Geom g, int *parent, unsigned *err)
+{
+    GlobalAcc acc{gval, parent, err, g.N};
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
+         p += (long long)gridDim.x * blockDim.x) {
+        int r = levelroot(acc, (int)p);
+        if (r != (int)p) acc.set_par((int)p, r);
+    }
+}
+
+__global__ void k_canon_roots(const float *__restrict__ gval, Geom g, int *parent, unsigned char *isroot,
+                              unsigned long long *num_nodes, unsigned *err)
+{
+    GlobalAcc acc{gval, parent, err, g.N};
+    unsigned cnt = 0;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
+         p += (long long)gridDim.x * blockDim.x) {
+        int q = acc.par((int)p);
+        uint32_t kp = acc.key((int)p);
+        const bool root = q == NONE || acc.key(q) != kp;
+        isroot[p] = root ? 1 : 0;
+        if (root) {
+            cnt++;
+            if (q != NONE) {
+                int r = acc.par(q);
+                if (r != NONE && acc.key(r) == acc.key(q)) acc.set_par((int)p, r);
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(num_nodes, (unsigned long long)cnt);
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------
+template <typename T, bool MIN>
+static void build_t(const BuildArgs &a, cudaStream_t s)
+{
+    const T *img = (const T *)a.img;
+    const bool is3d = a.g.D > 1;
+    const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
+    dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
+    k_tile_build<T, MIN><<<grid, TILE_THREADS, 0, s>>>(img, a.g, a.kmax, a.gval, a.parent, a.err);
+    int nb = grid_for(a.g.N, 256, a.sm_count);
+    k_seam_merge<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.err);
+    k_canon_pixels<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.err);
+    k_canon_roots<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.isroot, a.num_nodes, a.err);
+}
+
+void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsigned *kmax, unsigned *nans,
+                  int sm_count, cudaStream_t s)
+{
+    int nb = grid_for(n, 256, sm_count);
+    switch (dtype) {
+    case U8: k_stats<uint8_t><<<nb, 256, 0, s>>>((const uint8_t *)img, n, kmin, kmax, nans); break;
+    case U16: k_stats<uint16_t><<<nb, 256, 0, s>>>((const uint16_t *)img, n, kmin, kmax, nans); break;
+    case U32: k_stats<uint32_t><<<nb, 256, 0, s>>>((const uint32_t *)img, n, kmin, kmax, nans); break;
+    default: k_stats<float><<<nb, 256, 0, s>>>((const float *)img, n, kmin, kmax, nans); break;
+    }
+}
+
+void launch_build(const BuildArgs &a, cudaStream_t s)
+{
+    switch (a.dtype * 2 + (a.tree_min ? 1 : 0)) {
+    case 0: build_t<uint8_t, false>(a, s); break;
+    case 1: build_t<uint8_t, true>(a, s); break;
+    case 2: build_t<uint16_t, false>(a, s); break;
+    case 3: build_t<uint16_t, true>(a, s); break;
+    case 4: build_t<uint32_t, false>(a, s); break;
+    case 5: build_t<uint32_t, true>(a, s); break;
+    case 6: build_t<float, false>(a, s); break;
+    default: build_t<float, true>(a, s); break;
+    }
+}
+
+}  // namespace dcf

@@ -1,0 +1,176 @@
+// Internal device/host definitions shared by the CUDA translation units.
+//
+// Data layout in HBM (one tree):
+//   img      caller's pixels in their own type (u8/u16/u32/f32), x fastest;
+//            grey levels and sort keys are recomputed from it on the fly, so no
+//            per-pixel level or key array is stored.
+//   parent   int32[N]: canonical form after the build -- a pixel that is not a
+//            level root points to its node's level root (the lowest linear index
+//            of the node's flat zone, the reference's choice, flood.c:127-141); a
+//            level root points to its parent node's level root; the root holds -1.
+//   attribute records: structure-of-arrays indexed by pixel, valid at level roots.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dcf_eigen.h"
+
+namespace dcf {
+
+constexpr int NONE = -1;
+
+enum DType : int { U8 = 0, U16 = 1, U32 = 2, F32 = 3 };
+
+// Error bits raised by kernels into a device word the host checks.
+enum DevErr : unsigned {
+    DEVERR_MERGE_BOUND = 1u << 0,   // a merge loop exceeded its iteration bound
+    DEVERR_WALK_BOUND = 1u << 1,    // a tree walk exceeded its iteration bound
+    DEVERR_WAIT_BOUND = 1u << 2,    // a bounded wait gave up (work queue / flag)
+};
+
+struct Geom {
+    int W, H, D;
+    long long WH;
+    long long N;
+    int conn;
+};
+
+// Grey level as the reference holds it (types.h:53 `value` = float): the pixel
+// converted to float, inverted as max - v for a min-tree (preprocessing.c:84-91).
+template <typename T>
+__device__ __forceinline__ float to_float(T v);
+template <> __device__ __forceinline__ float to_float<uint8_t>(uint8_t v) { return (float)v; }
+template <> __device__ __forceinline__ float to_float<uint16_t>(uint16_t v) { return (float)v; }
+template <> __device__ __forceinline__ float to_float<uint32_t>(uint32_t v) { return __uint2float_rn(v); }
+template <> __device__ __forceinline__ float to_float<float>(float v) { return v; }
+
+template <typename T, bool MIN>
+__device__ __forceinline__ float level_of(T raw, float gmax)
+{
+    float v = to_float<T>(raw);
+    return MIN ? __fsub_rn(gmax, v) : v;
+}
+
+// Order-preserving unsigned key of a float level (the reference's transform_float,
+// flood.c:362-371).  -0.0 is folded onto +0.0 first because the reference treats
+// them as one grey level (its flat-zone test is float ==).
+__device__ __forceinline__ uint32_t order_key(float v)
+{
+    uint32_t u = __float_as_uint(v);
+    if (u == 0x80000000u) u = 0u;
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float key_to_level(uint32_t k)
+{
+    uint32_t u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+    return __uint_as_float(u);
+}
+
+// Forward half-neighbourhoods (offsets with a larger linear index) per connectivity.
+// 2-D 4: +x, +y.  2-D 8: +x, +y, (+1,+1), (-1,+1).  3-D 6: +x, +y, +z.
+// 3-D 26: the 13 offsets (dx,dy,dz) lexicographically after (0,0,0).
+struct Offs {
+    int n;
+    signed char d[13][3];
+};
+
+__host__ __device__ inline Offs forward_offsets(int conn)
+{
+    Offs o{};
+    auto add = [&](int dx, int dy, int dz) {
+        o.d[o.n][0] = (signed char)dx;
+        o.d[o.n][1] = (signed char)dy;
+        o.d[o.n][2] = (signed char)dz;
+        o.n++;
+    };
+    if (conn == 4 || conn == 6 || conn == 8) {
+        add(1, 0, 0);
+        add(0, 1, 0);
+        if (conn == 6) add(0, 0, 1);
+        if (conn == 8) {
+            add(1, 1, 0);
+            add(-1, 1, 0);
+        }
+    } else {  // 26
+        for (int dz = 0; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    if (dz == 0 && (dy < 0 || (dy == 0 && dx <= 0))) continue;
+                    add(dx, dy, dz);
+                }
+    }
+    return o;
+}
+
+// ---------------------------------------------------------------------------
+// Lock-free concurrent merge of two branches of a max-tree forest.
+//
+// Invariant kept by every writer: par[x] is NONE, or key(par[x]) <= key(x), and
+// a link between equal keys goes to a LOWER index.  A pixel x is a level root iff
+// par[x] == NONE or key(par[x]) < key(x); following equal-key links from any
+// pixel ends at the lowest index of its flat zone.
+//
+// connect(a, b) makes the root paths of a and b one sorted chain (the merge of
+// Wilkinson et al.'s concurrent filter, the reference's merge_nodes flood.c:292-353),
+// but without locks: the only write that changes structure is a CAS that splices
+// node b between a and a's parent pa (key(pa) < key(b) <= key(a)); the displaced
+// tail pa is then merged into b's chain by the same thread.  Every successful CAS
+// raises par[a]'s key, so the loop terminates; links are only ever created between
+// pixels connected at or above the lower key, so at quiescence the forest is the
+// component tree of all merged edges.  Path halving writes only shortcut
+// equal-key links, which no CAS can race with (a CAS expects a lower-key parent).
+// ---------------------------------------------------------------------------
+template <class A>
+__device__ __forceinline__ int levelroot(A &acc, int i)
+{
+    const uint32_t k = acc.key(i);
+    const long long bound = acc.walk_bound();
+    for (long long it = 0; it < bound; it++) {
+        int p = acc.par(i);
+        if (p == NONE || acc.key(p) != k) return i;
+        int pp = acc.par(p);
+        if (pp != NONE && acc.key(pp) == k) acc.set_par(i, pp);
+        i = p;
+    }
+    acc.error(DEVERR_WALK_BOUND);
+    return i;
+}
+
+template <class A>
+__device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
+{
+    for (long long it = 0; it < bound; it++) {
+        a = levelroot(acc, a);
+        b = levelroot(acc, b);
+        if (a == b) return;
+        uint32_t ka = acc.key(a), kb = acc.key(b);
+        if (ka < kb || (ka == kb && a < b)) {
+            int t = a; a = b; b = t;
+            uint32_t tk = ka; ka = kb; kb = tk;
+        }
+        // a sits above b: ka > kb, or equal keys with a > b (a's node joins b's)
+        int pa = acc.par(a);
+        if (pa != NONE) {
+            int lpa = levelroot(acc, pa);
+            if (lpa == b) return;
+            if (acc.key(lpa) >= kb) {  // b belongs below a's parent node: descend
+                a = lpa;
+                continue;
+            }
+        }
+        if (acc.cas_par(a, pa, b)) {
+            if (pa == NONE) return;
+            a = b;
+            b = pa;
+        }
+    }
+    acc.error(DEVERR_MERGE_BOUND);
+}
+
+__device__ __forceinline__ void raise_error(unsigned *err, unsigned bit)
+{
+    if (err) atomicOr(err, bit);
+}
+
+}  // namespace dcf

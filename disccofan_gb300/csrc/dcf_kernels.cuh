@@ -1,0 +1,90 @@
+// Launch interface between the C-ABI layer (dcf_api.cu) and the kernel units.
+#pragma once
+#include "dcf_internal.cuh"
+
+namespace dcf {
+
+constexpr int TILE_THREADS = 256;
+constexpr int TILE_PIX = 4096;                 // 64x64 (2-D) or 16x16x16 (3-D)
+constexpr long long MERGE_BOUND_SMEM = 1LL << 22;
+constexpr long long MERGE_BOUND_GLOBAL = 1LL << 28;
+
+inline int grid_for(long long n, int block, int sm_count)
+{
+    long long b = (n + block - 1) / block;
+    long long cap = (long long)sm_count * 32;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+struct BuildArgs {
+    int dtype;
+    bool tree_min;
+    const void *img;
+    Geom g;
+    const unsigned *kmax;            // order key of the maximum level (min-tree inversion)
+    float *gval;
+    int *parent;
+    unsigned char *isroot;
+    unsigned long long *num_nodes;
+    unsigned *err;
+    int sm_count;
+};
+
+void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsigned *kmax, unsigned *nans,
+                  int sm_count, cudaStream_t s);
+void launch_build(const BuildArgs &a, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// attribute records (structure of arrays over pixels; valid at level roots)
+// ---------------------------------------------------------------------------
+struct AttrBufs {
+    int group = -1;
+    bool exact_g = false;            // grey-weighted sums kept as exact integers (u8/u16)
+    uint32_t *area = nullptr;
+    uint32_t *bmin[3] = {nullptr, nullptr, nullptr};
+    uint32_t *bmax[3] = {nullptr, nullptr, nullptr};
+    unsigned long long *s1[3] = {nullptr, nullptr, nullptr};   // sum x, y, z
+    unsigned long long *s2[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // x2 y2 z2 xy yz xz
+    void *gw[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // sum g, g^2, g*x, g*y, g*z (i64 or f64)
+    int *pending = nullptr;          // children not yet folded in (bottom-up pass)
+};
+
+struct TreeView {
+    Geom g;
+    bool tree_min;
+    const unsigned *kmax;            // device: order key of the input's maximum
+    const float *gval;
+    const int *parent;
+    const unsigned char *isroot;
+    float pixdim[3];
+};
+
+void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm_count, cudaStream_t s);
+
+// attribute readout of every level root into a double array (NaN elsewhere)
+void launch_node_attr(const TreeView &t, const AttrBufs &a, int attr, bool area, double *out, int sm_count,
+                      cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// operations
+// ---------------------------------------------------------------------------
+struct FilterWork {
+    unsigned char *flag = nullptr;  // per pixel: survive bit (valid at level roots)
+    int *target = nullptr;          // per pixel: resolved node / topmost removed ancestor
+    unsigned *kept = nullptr;       // max rule: node has a surviving descendant-or-self
+    int *jump = nullptr, *jump2 = nullptr;   // pointer-jumping double buffers
+    int *best2 = nullptr;
+    double *acc = nullptr, *acc2 = nullptr;
+};
+
+void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, double lambda, bool extract,
+                   float *out, const FilterWork &w, long long depth_bound, unsigned *err, int sm_count,
+                   cudaStream_t s);
+void launch_check(const TreeView &t, const AttrBufs &a, int attr, float *out, int sm_count, cudaStream_t s);
+void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *l1, int n1, int a2,
+                     const float *l2, int n2, double *spec, int sm_count, cudaStream_t s);
+void launch_level_out(const TreeView &t, float *out, int sm_count, cudaStream_t s);
+
+}  // namespace dcf

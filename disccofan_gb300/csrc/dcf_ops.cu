@@ -1,0 +1,301 @@
+// Operations on a built tree (the reference's filtering.c, pattern.c and the
+// per-pixel parts of operation.c), re-designed as node-parallel passes:
+//
+//   k_flag          survive bit of every level root: attribute >= lambda.
+//   k_resolve       each node finds its nearest flagged ancestor-or-self by walking
+//                   up; results are written back along the walked path so later
+//                   walkers stop early (direct and max rules, filtering.c:102,156).
+//   k_mark_kept     max rule: every survivor marks its ancestors as kept.
+//   k_jump_*        pointer jumping over root paths with double buffers: path sums
+//                   for the subtractive rule (filtering.c:211-261) and the topmost
+//                   removed ancestor for the min rule (filtering.c:55-100).
+//   k_filter_out    per pixel: value of its node's resolution, then extract
+//                   (gval - out) and min-tree re-inversion (g_max - out),
+//                   operation.c:17-28.
+//   k_check         per pixel: (float) attribute of its node (filtering.c:47-52).
+//   k_spectrum      per level root: dh = gval - gval(parent) in float, bins by
+//                   binary search (pattern.c:7-24), dh * area accumulated in a
+//                   shared-memory histogram per block, flushed with global atomics.
+#include "dcf_kernels.cuh"
+#include "dcf_attr_eval.cuh"
+
+namespace dcf {
+
+constexpr int UNKNOWN = -2;
+
+#define GRID_LOOP(p, n) \
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < (n); p += (long long)gridDim.x * blockDim.x)
+
+__global__ void k_flag(Geom g, const unsigned char *__restrict__ isroot, AttrBufs a, int attr, double lambda,
+                       float pd0, float pd1, float pd2, unsigned char *flag, int *target)
+{
+    const float pd[3] = {pd0, pd1, pd2};
+    GRID_LOOP(p, g.N)
+    {
+        target[p] = UNKNOWN;
+        if (!isroot[p]) continue;
+        flag[p] = attr_value(a, attr, (int)p, pd) >= lambda ? 1 : 0;
+    }
+}
+
+__global__ void k_mark_kept(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                            const unsigned char *__restrict__ flag, unsigned *kept, unsigned *err)
+{
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p] || !flag[p]) continue;
+        int u = (int)p;
+        long long it = 0;
+        for (; it < g.N && u != NONE; it++) {
+            if (atomicExch(kept + u, 1u) == 1u) break;
+            u = parent[u];
+        }
+        if (it >= g.N) raise_error(err, DEVERR_WALK_BOUND);
+    }
+}
+
+// nearest flagged ancestor-or-self; flag may be a byte array or the kept words
+template <typename F>
+__global__ void k_resolve(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                          const F *__restrict__ flag, int *target, unsigned *err)
+{
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p]) continue;
+        if (((volatile int *)target)[p] != UNKNOWN) continue;
+        int v = (int)p, res = NONE;
+        long long it = 0;
+        for (; it < g.N; it++) {
+            int t = ((volatile int *)target)[v];
+            if (t != UNKNOWN) { res = t; break; }
+            if (flag[v]) { res = v; break; }
+            int q = parent[v];
+            if (q == NONE) { res = NONE; break; }
+            v = q;
+        }
+        if (it >= g.N) raise_error(err, DEVERR_WALK_BOUND);
+        for (int w = (int)p; w != v; w = parent[w]) ((volatile int *)target)[w] = res;
+        ((volatile int *)target)[v] = res;
+    }
+}
+
+// subtractive: value(u) = sum over the root path of delta(w), delta(w) =
+// flag ? gval(w) - gval(parent(w)) : 0, the root's delta being flag ? gval : 0.
+__global__ void k_sub_init(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                           const float *__restrict__ gval, const unsigned char *__restrict__ flag, int *jump,
+                           double *acc)
+{
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p]) continue;
+        int q = parent[p];
+        jump[p] = q;
+        double d = 0.0;
+        if (flag[p]) d = q == NONE ? (double)gval[p] : (double)gval[p] - (double)gval[q];
+        acc[p] = d;
+    }
+}
+
+__global__ void k_jump_sum(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ jin,
+                           const double *__restrict__ ain, int *jout, double *aout)
+{
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p]) continue;
+        int j = jin[p];
+        if (j == NONE) {
+            jout[p] = NONE;
+            aout[p] = ain[p];
+        } else {
+            jout[p] = jin[j];
+            aout[p] = ain[p] + ain[j];
+        }
+    }
+}
+
+// min rule: best(u) = topmost removed node on u's path, root excluded
+__global__ void k_min_init(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                           const unsigned char *__restrict__ flag, int *jump, int *best)
+{
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p]) continue;
+        int q = parent[p];
+        jump[p] = q;
+        best[p] = (q != NONE && !flag[p]) ? (int)p : NONE;
+    }
+}
+
+__global__ void k_jump_last(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ jin,
+                            const int *__restrict__ bin, int *jout, int *bout)
+{
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p]) continue;
+        int j = jin[p];
+        if (j == NONE) {
+            jout[p] = NONE;
+            bout[p] = bin[p];
+        } else {
+            jout[p] = jin[j];
+            int bj = bin[j];
+            bout[p] = bj != NONE ? bj : bin[p];
+        }
+    }
+}
+
+template <int RULE>
+__global__ void k_filter_out(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                             const float *__restrict__ gval, const unsigned char *__restrict__ flag,
+                             const int *__restrict__ target, const double *__restrict__ acc, bool extract,
+                             bool tree_min, const unsigned *kmax, float *out)
+{
+    const float gmax = tree_min ? key_to_level(*kmax) : 0.0f;
+    GRID_LOOP(p, g.N)
+    {
+        const int node = isroot[p] ? (int)p : parent[p];
+        float val;
+        if (RULE == 0 || RULE == 2) {
+            int s = target[node];
+            val = s >= 0 ? gval[s] : 0.0f;
+        } else if (RULE == 3) {
+            val = (float)acc[node];
+        } else {  // min
+            int r = target[node];
+            if (r != NONE) val = gval[parent[r]];
+            else if (parent[node] == NONE) val = flag[node] ? gval[node] : 0.0f;
+            else val = gval[node];
+        }
+        if (extract) val = __fsub_rn(gval[p], val);
+        if (tree_min) val = __fsub_rn(gmax, val);
+        out[p] = val;
+    }
+}
+
+static int rounds_for(long long depth_bound)
+{
+    int r = 0;
+    while ((1LL << r) <= depth_bound && r < 40) r++;
+    return r;
+}
+
+void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, double lambda, bool extract,
+                   float *out, const FilterWork &w, long long depth_bound, unsigned *err, int sm, cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+    k_flag<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
+                              w.target);
+    const double *accp = nullptr;
+    if (rule == 0) {
+        k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err);
+    } else if (rule == 2) {
+        cudaMemsetAsync(w.kept, 0, t.g.N * sizeof(unsigned), s);
+        k_mark_kept<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.kept, err);
+        k_resolve<unsigned><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.kept, w.target, err);
+    } else {
+        const int R = rounds_for(depth_bound);
+        int *j0 = w.jump, *j1 = w.jump2;
+        if (rule == 3) {
+            double *a0 = w.acc, *a1 = w.acc2;
+            k_sub_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, j0, a0);
+            for (int r = 0; r < R; r++) {
+                k_jump_sum<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, a0, j1, a1);
+                int *tj = j0; j0 = j1; j1 = tj;
+                double *ta = a0; a0 = a1; a1 = ta;
+            }
+            accp = a0;
+        } else {
+            int *b0 = w.target, *b1 = w.best2;
+            k_min_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, j0, b0);
+            for (int r = 0; r < R; r++) {
+                k_jump_last<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, b0, j1, b1);
+                int *tj = j0; j0 = j1; j1 = tj;
+                int *tb = b0; b0 = b1; b1 = tb;
+            }
+            if (b0 != w.target) cudaMemcpyAsync(w.target, b0, t.g.N * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        }
+    }
+#define DCF_OUT(R) \
+    k_filter_out<R><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, w.target, accp, extract, t.tree_min, t.kmax, out)
+    switch (rule) {
+    case 0: DCF_OUT(0); break;
+    case 1: DCF_OUT(1); break;
+    case 2: DCF_OUT(2); break;
+    default: DCF_OUT(3); break;
+    }
+#undef DCF_OUT
+}
+
+__global__ void k_check(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent, AttrBufs a,
+                        int attr, float pd0, float pd1, float pd2, float *out)
+{
+    const float pd[3] = {pd0, pd1, pd2};
+    GRID_LOOP(p, g.N)
+    {
+        const int node = isroot[p] ? (int)p : parent[p];
+        out[p] = (float)attr_value(a, attr, node, pd);
+    }
+}
+
+void launch_check(const TreeView &t, const AttrBufs &a, int attr, float *out, int sm, cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+    k_check<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, a, attr, t.pixdim[0], t.pixdim[1], t.pixdim[2], out);
+}
+
+// find_scale (pattern.c:7-24): the last bin whose lambda is <= the attribute
+__device__ __forceinline__ int find_scale(const float *lv, int n, double v)
+{
+    int upper = n - 1, lower = 0;
+    if (v >= (double)lv[upper]) return upper;
+    int mid = (upper + lower) / 2;
+    while (mid != lower) {
+        if (v >= (double)lv[mid]) lower = mid;
+        else upper = mid;
+        mid = (upper + lower) / 2;
+    }
+    return lower;
+}
+
+constexpr int SPEC_SMEM_BINS = 4096;
+
+__global__ void k_spectrum(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                           const float *__restrict__ gval, AttrBufs a, int a1, const float *__restrict__ l1, int n1,
+                           int a2, const float *__restrict__ l2, int n2, float pd0, float pd1, float pd2,
+                           double *spec)
+{
+    __shared__ double hist[SPEC_SMEM_BINS];
+    const int nbins = n1 * n2;
+    const bool priv = nbins <= SPEC_SMEM_BINS;
+    if (priv)
+        for (int i = threadIdx.x; i < nbins; i += blockDim.x) hist[i] = 0.0;
+    __syncthreads();
+    const float pd[3] = {pd0, pd1, pd2};
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p]) continue;
+        const int q = parent[p];
+        const float dh = q != NONE ? __fsub_rn(gval[p], gval[q]) : gval[p];
+        if (dh == 0.0f) continue;
+        const double ar = area_value(a, (int)p, pd);
+        const int s1 = find_scale(l1, n1, a1 < 0 ? ar : attr_value(a, a1, (int)p, pd));
+        const int s2 = n2 <= 1 ? 0 : find_scale(l2, n2, a2 < 0 ? ar : attr_value(a, a2, (int)p, pd));
+        const double v = (double)dh * ar;
+        if (priv) atomicAdd(hist + s1 + s2 * n1, v);
+        else atomicAdd(spec + s1 + s2 * n1, v);
+    }
+    if (!priv) return;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+        if (hist[i] != 0.0) atomicAdd(spec + i, hist[i]);
+}
+
+void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *l1, int n1, int a2, const float *l2,
+                     int n2, double *spec, int sm, cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+    k_spectrum<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
+                                  t.pixdim[1], t.pixdim[2], spec);
+}
+
+}  // namespace dcf

@@ -1,0 +1,138 @@
+/*
+ * dcf.h -- C ABI of the GB300 component-forest library (libdcf_gb300.so).
+ *
+ * Drop-in for the hot path of disccofan: max/min-tree construction, attribute
+ * accumulation, attribute filtering and pattern spectra.  Plain C types only; every
+ * call returns a dcf_status.  Pixels are in x-fastest order (index = x + y*W +
+ * z*W*H), the same order the reference's Node.gval uses.  A pointer argument is a
+ * HOST pointer unless the call's on_device flag says it is a device pointer.
+ *
+ * Reference interfaces each call replaces (paths relative to the reference repo):
+ *   dcf_tree_build            build_tree_with_attributes      src/sources/flood.c:175
+ *                             (with preprocessing's min-tree inversion,
+ *                              src/sources/preprocessing.c:77-91, and io.c:64-79's
+ *                              connectivity fix-ups)
+ *   dcf_tree_set_attribute    flood_attributes                src/sources/flood.c:184
+ *   dcf_tree_parent           Node.parent after the build (types.h:147-159) /
+ *                             get_levelroot                   src/sources/flood.c:693
+ *   dcf_node_attribute        AttribsArray[i].attribute/.area src/sources/attributes.c:1224
+ *   dcf_filter                tree_filtering + perform_filter_or_extract
+ *                                                             src/sources/filtering.c:18,
+ *                                                             src/sources/operation.c:10
+ *   dcf_attribute_check       tree_attribute_check            src/sources/filtering.c:47
+ *   dcf_pattern_spectrum      tree_pattern_spectrum           src/sources/pattern.c:27
+ *   dcf_pattern_spectrum2d    tree_pattern_spectrum2d (+ the attribute-order rule of
+ *                             perform_pattern_spectrum)       src/sources/pattern.c:110,
+ *                                                             src/sources/operation.c:88-100
+ *   dcf_dmp                   perform_dmp_operation           src/sources/operation.c:63
+ *   dcf_lvec_read             lambda_vector_read              src/sources/lambdavec.c:35
+ *   dcf_batch_*               (no reference counterpart: many cutouts per launch)
+ *   dcf_adjoint_*             (no reference counterpart: gradients for float images)
+ */
+#ifndef DCF_H
+#define DCF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DCF_OK = 0,
+    DCF_ERR_INVALID = 1,     /* bad argument (dims, connectivity, attribute, rule, sizes) */
+    DCF_ERR_NOMEM = 2,       /* device or host allocation failed */
+    DCF_ERR_CUDA = 3,        /* a CUDA call failed; dcf_ctx_last_error has the text */
+    DCF_ERR_TIMEOUT = 4,     /* a bounded device loop gave up (merge/walk/wait bound) */
+    DCF_ERR_NAN = 5,         /* the image holds NaN: its grey levels are unordered */
+    DCF_ERR_STATE = 6,       /* call not valid in the object's current state */
+    DCF_ERR_IO = 7,          /* file could not be read or parsed */
+    DCF_ERR_UNSUPPORTED = 8  /* valid request this build does not implement */
+} dcf_status;
+
+typedef enum { DCF_U8 = 0, DCF_U16 = 1, DCF_U32 = 2, DCF_F32 = 3 } dcf_dtype;
+typedef enum { DCF_MAX_TREE = 0, DCF_MIN_TREE = 1 } dcf_tree_type;
+/* filter rules, in the reference's Decisions[] order (filtering.c:271-277) */
+typedef enum { DCF_RULE_DIRECT = 0, DCF_RULE_MIN = 1, DCF_RULE_MAX = 2, DCF_RULE_SUBTRACTIVE = 3 } dcf_rule;
+
+/* Attribute indices 0..17 are the reference's AttribsArray (attributes.c:1224-1248):
+ * 0 area | 1 rectarea 2 rectdiag 3 xext 4 yext 5 zext | 6 xmean 7 ymean 8 zmean |
+ * 9 xwmean 10 ywmean 11 zwmean 12 flux | 13 inertia trace 14 elongation 15 flatness
+ * 16 sparseness 17 non-compactness.  18 = bounding-box elongation
+ * max(xext,yext)/max(min(xext,yext),1) on the extent group (not in the reference). */
+#define DCF_NUM_ATTRIBUTES 19
+
+typedef struct dcf_ctx dcf_ctx;
+typedef struct dcf_tree dcf_tree;
+
+typedef struct {
+    const void *data;        /* pixels, x fastest */
+    int dtype;               /* dcf_dtype */
+    int on_device;           /* 1: data is a device pointer on the context's device */
+    uint64_t dims[3];        /* width, height, depth (depth = 1 for 2-D) */
+    int connectivity;        /* 4 or 8 (2-D), 6 or 26 (3-D); fixed up like io.c:64-79 */
+    int tree_type;           /* dcf_tree_type */
+    float pixdim[3];         /* physical pixel size (config pixel_dim); 1,1,1 usual */
+} dcf_image;
+
+/* ---- context: one device, one stream, a reusable device workspace ---- */
+dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out);
+dcf_status dcf_ctx_destroy(dcf_ctx *ctx);
+dcf_status dcf_ctx_synchronize(dcf_ctx *ctx);
+const char *dcf_ctx_last_error(const dcf_ctx *ctx);
+const char *dcf_status_string(dcf_status s);
+/* number of device kernel launches issued through this context so far */
+uint64_t dcf_ctx_launch_count(const dcf_ctx *ctx);
+
+/* ---- tree ---- */
+/* Build the max-tree (min-tree: of the inverted image) with the attribute group
+ * of attr_idx.  The image is copied to the device when on_device == 0. */
+dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_tree **out);
+/* Accumulate the attribute group of attr_idx on the existing tree (no rebuild). */
+dcf_status dcf_tree_set_attribute(dcf_ctx *ctx, dcf_tree *tree, int attr_idx);
+dcf_status dcf_tree_destroy(dcf_tree *tree);
+dcf_status dcf_tree_info(const dcf_tree *tree, uint64_t *num_pixels, uint64_t *num_nodes, int *connectivity,
+                         float *max_gval);
+/* Canonical parent array: a pixel that is not a level root -> its node's level
+ * root (the lowest index of the node's flat zone); a level root -> its parent
+ * node's level root; the root -> -1.  Bit-identical to the reference's
+ * sequential Node.parent after build_tree_with_attributes. */
+dcf_status dcf_tree_parent(dcf_ctx *ctx, dcf_tree *tree, int64_t *parent, int on_device);
+/* Grey levels the tree was built on (float; inverted for a min-tree). */
+dcf_status dcf_tree_gval(dcf_ctx *ctx, dcf_tree *tree, float *gval, int on_device);
+/* Attribute (area=0) or group area readout (area=1) of every level root; NaN at
+ * other pixels.  attr_idx must belong to the tree's current attribute group. */
+dcf_status dcf_node_attribute(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, int area, double *out, int on_device);
+
+/* ---- operations ---- */
+/* tree_filtering with rule, then extract (gval - out) when extract != 0, then the
+ * min-tree re-inversion g_max - out.  out: width*height*depth floats. */
+dcf_status dcf_filter(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, int rule, double lambda, int extract,
+                      float *out, int on_device);
+/* out[p] = (float) attribute of p's node. */
+dcf_status dcf_attribute_check(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, float *out, int on_device);
+/* Differential morphological profile: for each lvec[i+1], i < num_lambdas-1,
+ * out[i*N + p] = gval - filter(lvec[i+1]). */
+dcf_status dcf_dmp(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, int rule, const float *lvec, int num_lambdas,
+                   float *out, int on_device);
+/* 1-D pattern spectrum; lvec holds num_lambdas bins INCLUDING the leading 0 (the
+ * output of dcf_lvec_read).  spectrum[num_lambdas] is ACCUMULATED (+=), as the
+ * reference accumulates into a caller-zeroed array (pattern.c:98-105). */
+dcf_status dcf_pattern_spectrum(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, const float *lvec, int num_lambdas,
+                                double *spectrum, int on_device);
+/* 2-D pattern spectrum, spectrum[s1 + s2*n1] accumulated.  As in the reference,
+ * attr1 must be the higher index unless attr2 is 0, and attr2 == 0 bins by the
+ * first attribute group's area. */
+dcf_status dcf_pattern_spectrum2d(dcf_ctx *ctx, dcf_tree *tree, int attr1, const float *lvec1, int n1, int attr2,
+                                  const float *lvec2, int n2, double *spectrum, int on_device);
+
+/* ---- lambda vectors ---- */
+/* Read a "#LambdaVector file..." file: out[0] = 0, out[i] = value_i / imscale.
+ * *num_lambdas receives K+1; fails with DCF_ERR_INVALID if capacity < K+1. */
+dcf_status dcf_lvec_read(const char *path, double imscale, float *out, int capacity, int *num_lambdas);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

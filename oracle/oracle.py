@@ -301,6 +301,7 @@ class Port:
         return out
 
     def node_attr(self, attr: int, area: bool = False) -> np.ndarray:
+        self.prepare(attr)
         out = np.empty(self.n, np.float64)
         if self.lib.dco_node_attr(self.t, attr, int(area), out.ctypes.data) != 0:
             raise RuntimeError("node_attr failed")

@@ -1,0 +1,68 @@
+"""CPU tests of the C-ABI library: it loads, exports every symbol include/*.h
+declares, and its host-only entry points behave like the reference's."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(dcf_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import disccofan_gb300 as dcf
+    return dcf.library()
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("dcf_tree_build", "dcf_filter", "dcf_pattern_spectrum2d", "dcf_tree_parent", "dcf_lvec_read"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_lvec_read_matches_reference_semantics(tmp_path):
+    import disccofan_gb300 as dcf
+    p = tmp_path / "lvec.txt"
+    p.write_text("#LambdaVector file. Keep this exact line in all similar lambda vector files\n"
+                 "100\n1000\n10000\n50000\n100000\n150000\n\n")
+    got = dcf.read_lvec(str(p), 3.0)
+    want = dcf.lvec_from_values([100, 1000, 10000, 50000, 100000, 150000], 3.0)
+    assert np.array_equal(got, want)
+    assert got[0] == 0 and got.size == 7
+
+
+def test_lvec_read_errors(tmp_path):
+    import disccofan_gb300 as dcf
+    with pytest.raises(dcf.DcfError):
+        dcf.read_lvec(str(tmp_path / "missing.txt"))
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1\n2\n")
+    with pytest.raises(dcf.DcfError):
+        dcf.read_lvec(str(bad))
+
+
+def test_ctx_create_without_gpu_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    st = lib.dcf_ctx_create(0, None, C.byref(h))
+    assert st != 0 and not h.value

@@ -1,0 +1,153 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's own golden
+fixtures, the reference's outputs on synthetic inputs, and the CPU oracle.
+
+Tolerances: parents, integer attributes, filtered images and integer-image
+spectra are compared bit-exactly.  Grey-weighted moments of float images are
+accumulated in a different order than the reference (atomics vs flood order), so
+attributes derived from them (9-12, and the inertia sums of float images) are
+compared within 1e-9 relative; float-image spectra within 1e-9 relative."""
+import numpy as np
+import pytest
+
+import disccofan_gb300 as dcf
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+FLOAT_ATTR_RTOL = 1e-9
+
+
+def gpu_tree(ctx, img, conn, tree="max", attr=0):
+    return ctx.build(img, connectivity=conn, tree_type=tree, attribute=attr)
+
+
+def test_lena_filters_match_reference_fixtures(ctx, lena):
+    t = gpu_tree(ctx, lena["lena"], 4, attr=0)
+    assert np.array_equal(t.filter(0, 200.0).astype(np.uint8), lena["gt_area_200"])
+    assert np.array_equal(t.filter(17, 0.2).astype(np.uint8), lena["gt_ncomp_0_2"])
+
+
+def test_lena_checks_match_reference_fixtures(ctx, lena):
+    t = gpu_tree(ctx, lena["lena"], 4)
+    assert np.array_equal(t.check(0), lena["check_area_c4"])
+    assert np.array_equal(t.check(17), lena["check_ncomp_c4"])
+    t8 = gpu_tree(ctx, lena["lena"], 8)
+    assert np.array_equal(t8.check(0), lena["check_area_c8"])
+
+
+def test_lena_tree_matches_reference_tree_file(ctx, lena):
+    t = gpu_tree(ctx, lena["lena"], 4)
+    par = t.parent()
+    g = t.gval()
+    roots = np.nonzero((par < 0) | (g[np.maximum(par, 0)] != g))[0]
+    assert np.array_equal(roots, lena["tree_index"])
+    assert np.array_equal(par[roots], lena["tree_parent"])
+    assert np.array_equal(t.node_attribute(0)[roots].astype(np.int64), lena["tree_area"])
+    assert t.info()["nodes"] == roots.size
+
+
+@pytest.mark.parametrize("name", ["u8_2d_c4_max", "u8_2d_c8_min", "u16_2d_c8_max", "f32_2d_c4_max", "u8_3d_c6_max",
+                                  "u16_3d_c26_min", "f32_3d_c26_max"])
+def test_synthetic_reference_outputs(ctx, synthetic, name):
+    c = synthetic[name]
+    img = c["img"]
+    t = gpu_tree(ctx, img, int(c["conn"]), c["tree"].item().decode())
+    assert np.array_equal(t.parent(), c["parent"])
+    assert np.array_equal(t.node_attribute(0), c["area"], equal_nan=True)
+    for rule in (0, 3):
+        assert np.array_equal(t.filter(0, 12.0, rule), c[f"filter_area_r{rule}"]), rule
+    assert np.array_equal(t.filter(0, 12.0, 0, extract=True), c["extract_area"])
+    lv = dcf.lvec_from_values([2, 5, 10, 50, 200])
+    assert np.array_equal(t.pattern_spectrum(0, lv), c["pattern_area"])
+    exact = img.dtype != np.float32
+    for a in range(1, 18):
+        got, want = t.node_attribute(a), c[f"attr{a}"]
+        if exact or a < 9:
+            assert np.array_equal(got, want, equal_nan=True), a
+        else:
+            np.testing.assert_allclose(got, want, rtol=FLOAT_ATTR_RTOL, atol=1e-12, equal_nan=True, err_msg=str(a))
+    assert np.array_equal(t.filter(17, 0.3, 0), c["filter_ncomp_r0"])
+    l1 = dcf.lvec_from_values([1.2, 2, 4])
+    s2 = t.pattern_spectrum2d(14, l1, 0, lv)
+    if exact:
+        assert np.array_equal(s2, c["pattern2d_elong_area"])
+    else:
+        np.testing.assert_allclose(s2, c["pattern2d_elong_area"], rtol=FLOAT_ATTR_RTOL)
+
+
+def rand_image(rng, shape, kind):
+    if kind == "u8":
+        return rng.integers(0, 12, shape).astype(np.uint8)
+    if kind == "u16":
+        base = rng.integers(0, 3000, shape)
+        return (base // 7).astype(np.uint16)
+    if kind == "u32":
+        return rng.integers(0, 2**32 - 1, shape, dtype=np.uint64).astype(np.uint32)
+    return rng.standard_normal(shape).astype(np.float32)
+
+
+CASES = [((70, 130), "u8", 4, "max"), ((130, 70), "u8", 8, "min"), ((65, 64), "u16", 8, "max"),
+         ((200, 190), "u16", 4, "min"), ((33, 47), "f32", 4, "max"), ((129, 257), "f32", 8, "max"),
+         ((64, 64), "u32", 8, "max"), ((17, 18, 19), "u8", 6, "max"), ((20, 33, 17), "u16", 26, "min"),
+         ((16, 16, 16), "f32", 6, "max"), ((18, 17, 33), "f32", 26, "max"), ((1, 1), "u8", 4, "max"),
+         ((1, 300), "u16", 8, "max"), ((300, 1), "f32", 4, "min"), ((2, 3, 1), "u8", 26, "max")]
+
+
+@pytest.mark.parametrize("shape,kind,conn,tree", CASES)
+def test_random_against_oracle(ctx, shape, kind, conn, tree):
+    rng = np.random.default_rng(abs(hash((shape, kind, conn, tree))) % 2**32)
+    img = rand_image(rng, shape, kind)
+    port = oracle.Port()
+    port.load(img.astype(np.float32), conn, tree)
+    port.prepare(0)
+    t = gpu_tree(ctx, img, conn, tree)
+    assert np.array_equal(t.parent(), port.parent())
+    assert np.array_equal(t.gval(), port.gval())
+    assert np.array_equal(t.node_attribute(0), port.node_attr(0), equal_nan=True)
+    for rule in (0, 3):
+        lam = 5.0
+        assert np.array_equal(t.filter(0, lam, rule), port.filter(0, lam, rule)), rule
+    lv = dcf.lvec_from_values([2, 4, 16, 64])
+    want = port.pattern(0, [2, 4, 16, 64])
+    if kind == "f32":
+        np.testing.assert_allclose(t.pattern_spectrum(0, lv), want, rtol=1e-12)
+    else:
+        assert np.array_equal(t.pattern_spectrum(0, lv), want)
+    exact = kind in ("u8", "u16")
+    for a in (1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 16, 17, 18):
+        got, want = t.node_attribute(a), port.node_attr(a)
+        if exact or a < 9 or a == 18:
+            assert np.array_equal(got, want, equal_nan=True), a
+        else:
+            np.testing.assert_allclose(got, want, rtol=FLOAT_ATTR_RTOL, atol=1e-9, equal_nan=True, err_msg=str(a))
+
+
+def test_constant_image_single_node(ctx):
+    img = np.full((37, 91), 7, np.uint8)
+    t = gpu_tree(ctx, img, 8)
+    par = t.parent()
+    assert par[0] == -1 and np.all(par[1:] == 0)
+    assert t.info()["nodes"] == 1
+    assert np.all(t.filter(0, 10.0) == 7)
+
+
+def test_nan_rejected(ctx):
+    img = np.zeros((8, 8), np.float32)
+    img[3, 4] = np.nan
+    t = gpu_tree(ctx, img, 4)
+    with pytest.raises(dcf.DcfError) as e:
+        t.parent()
+    assert e.value.status == 5
+
+
+def test_bad_arguments(ctx):
+    with pytest.raises(dcf.DcfError) as e:
+        gpu_tree(ctx, np.zeros((4, 4), np.uint8), 5)
+    assert e.value.status == 1
+    with pytest.raises(dcf.DcfError):
+        gpu_tree(ctx, np.zeros((4, 4), np.uint8), 4, attr=19)
+    t = gpu_tree(ctx, np.zeros((4, 4), np.uint8), 4)
+    with pytest.raises(dcf.DcfError):
+        t.filter(0, 1.0, rule=7)
+    with pytest.raises(dcf.DcfError):
+        t.pattern_spectrum2d(0, dcf.lvec_from_values([1]), 3, dcf.lvec_from_values([1]))
