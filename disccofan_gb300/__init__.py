@@ -49,6 +49,18 @@ class _Image(C.Structure):
 
 
 _lib = None
+_exiting = False
+
+
+def _at_exit():
+    # objects finalised during interpreter shutdown must not call into CUDA
+    global _exiting
+    _exiting = True
+
+
+import atexit  # noqa: E402
+
+atexit.register(_at_exit)
 
 
 def library() -> C.CDLL:
@@ -131,9 +143,9 @@ class Context:
         self.device = device
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not _exiting:
             self.lib.dcf_ctx_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -203,9 +215,9 @@ class Tree:
         self.tree_type = tree_type
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not _exiting:
             self.ctx.lib.dcf_tree_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

@@ -143,8 +143,8 @@ dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out)
         ctx->own_stream = true;
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
-    if (cudaMalloc(&ctx->d_err, sizeof(unsigned)) != cudaSuccess ||
-        cudaMemset(ctx->d_err, 0, sizeof(unsigned)) != cudaSuccess) {
+    if (cudaMalloc(&ctx->d_err, 4 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(ctx->d_err, 0, 4 * sizeof(unsigned)) != cudaSuccess) {
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return DCF_ERR_NOMEM;
@@ -186,7 +186,7 @@ static void free_attr(dcf_tree *t)
 dcf_status dcf_tree_destroy(dcf_tree *t)
 {
     if (!t) return DCF_ERR_INVALID;
-    if (t->ctx) cudaStreamSynchronize(t->ctx->stream);
+    // cudaFree waits for the device; the context (and its stream) may already be gone
     free_attr(t);
     cudaFree(t->gval);
     cudaFree(t->parent);
@@ -206,6 +206,7 @@ static TreeView view_of(const dcf_tree *t)
     v.parent = t->parent;
     v.isroot = t->isroot;
     for (int i = 0; i < 3; i++) v.pixdim[i] = t->pixdim[i];
+    v.integer_levels = t->dtype == U8 || t->dtype == U16;
     return v;
 }
 
@@ -505,6 +506,7 @@ static dcf_status run_filter(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, 
             w.acc = (double *)p;
             if ((st = scratch(ctx, 6, N * 8, &p)) != DCF_OK) return st;
             w.acc2 = (double *)p;
+            w.remaining = ctx->d_err + 1;
         } else {
             if ((st = scratch(ctx, 5, N * 4, &p)) != DCF_OK) return st;
             w.best2 = (int *)p;

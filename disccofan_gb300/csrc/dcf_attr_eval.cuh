@@ -7,6 +7,62 @@
 
 namespace dcf {
 
+// ---- double-double helpers (Dekker / Knuth error-free transformations) ----
+struct dd {
+    double hi, lo;
+};
+__device__ __forceinline__ dd two_sum(double a, double b)
+{
+    double s = a + b, bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ dd two_prod(double a, double b)
+{
+    double p = a * b;
+    return {p, fma(a, b, -p)};
+}
+__device__ __forceinline__ dd dd_add(dd a, dd b)
+{
+    dd s = two_sum(a.hi, b.hi);
+    double lo = s.lo + a.lo + b.lo;
+    return two_sum(s.hi, lo);
+}
+__device__ __forceinline__ dd dd_mul(dd a, dd b)
+{
+    dd p = two_prod(a.hi, b.hi);
+    double lo = p.lo + (a.hi * b.lo + a.lo * b.hi);
+    return two_sum(p.hi, lo);
+}
+__device__ __forceinline__ dd dd_div_d(dd a, double b)
+{
+    double q1 = a.hi / b;
+    dd r = dd_add(a, two_prod(-q1, b));
+    double q2 = r.hi / b;
+    return two_sum(q1, q2);
+}
+
+// pow(x, 5.0/3.0) for x > 0 as glibc computes it (~0.52 ulp, i.e. correctly
+// rounded almost always).  The exponent is the double nearest 5/3, which exceeds
+// 5/3 by delta = 7.4014868308343770e-17, so x^e = x^(5/3) * (1 + delta*ln x + ...).
+// x^(5/3) is formed in double-double (Newton steps t <- t - (t^3 - x)/(3 t^2) for the
+// cube root, then x*t*t) and the delta term is added before the single final
+// rounding.  CUDA's own pow (2 ulp) would move non-compactness thresholds.
+__device__ __forceinline__ double pow_5_3(double x)
+{
+    const double delta = 7.4014868308343770e-17;
+    double t0 = cbrt(x);
+    dd t = {t0, 0.0};
+    for (int it = 0; it < 2; it++) {
+        dd t2 = dd_mul(t, t);
+        dd t3 = dd_mul(t2, t);
+        dd f = dd_add(t3, {-x, 0.0});
+        dd d = dd_div_d(f, 3.0 * t2.hi);
+        t = dd_add(t, {-d.hi, -d.lo});
+    }
+    dd r = dd_mul(dd_mul({x, 0.0}, t), t);
+    return r.hi + (r.lo + r.hi * (delta * log(x)));
+}
+
 __device__ __forceinline__ double gsum(const AttrBufs &a, int d, int u)
 {
     return a.exact_g ? (double)(long long)((const unsigned long long *)a.gw[d])[u] : ((const double *)a.gw[d])[u];
@@ -119,8 +175,9 @@ __device__ __forceinline__ double attr_value(const AttrBufs &a, int attr, int u,
         return M_PI * ax0 * ax1 * ax2 / (6 * in[0]);
     }
     case 17:
-        if (flat2d) return (mat[0] + mat[1]) / pow(in[0], 2.0);
-        return (mat[0] + mat[1] + mat[2]) / pow(in[0], 5.0 / 3.0);
+        // pow(area, 2.0) is exactly area*area whenever that is representable
+        if (flat2d) return (mat[0] + mat[1]) / (in[0] * in[0]);
+        return (mat[0] + mat[1] + mat[2]) / pow_5_3(in[0]);
     default:
         return __longlong_as_double(0x7ff8000000000000LL);
     }

@@ -166,7 +166,7 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
     for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
         int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
         if (lx >= wl || ly >= hl || lz >= dl) continue;
-        int r = levelroot(acc, i);
+        int r = levelroot_ro(acc, i);
         if (r != i) acc.set_par(i, r);
     }
     __syncthreads();
@@ -238,7 +238,7 @@ __global__ void k_canon_pixels(const float *__restrict__ gval, Geom g, int *pare
     GlobalAcc acc{gval, parent, err, g.N};
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
          p += (long long)gridDim.x * blockDim.x) {
-        int r = levelroot(acc, (int)p);
+        int r = levelroot_ro(acc, (int)p);
         if (r != (int)p) acc.set_par((int)p, r);
     }
 }

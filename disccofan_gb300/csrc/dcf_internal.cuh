@@ -137,6 +137,23 @@ __device__ __forceinline__ int levelroot(A &acc, int i)
     return i;
 }
 
+// Read-only level-root walk for the final canonicalisation passes: there every
+// thread writes only its own entry, because a path-halving write from another
+// thread could land after a fully compressed one and undo it.
+template <class A>
+__device__ __forceinline__ int levelroot_ro(A &acc, int i)
+{
+    const uint32_t k = acc.key(i);
+    const long long bound = acc.walk_bound();
+    for (long long it = 0; it < bound; it++) {
+        int p = acc.par(i);
+        if (p == NONE || acc.key(p) != k) return i;
+        i = p;
+    }
+    acc.error(DEVERR_WALK_BOUND);
+    return i;
+}
+
 template <class A>
 __device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
 {

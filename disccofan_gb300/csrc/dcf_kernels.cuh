@@ -59,6 +59,7 @@ struct TreeView {
     const int *parent;
     const unsigned char *isroot;
     float pixdim[3];
+    bool integer_levels;             // u8/u16 input: level arithmetic is exact in float
 };
 
 void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm_count, cudaStream_t s);
@@ -77,6 +78,7 @@ struct FilterWork {
     int *jump = nullptr, *jump2 = nullptr;   // pointer-jumping double buffers
     int *best2 = nullptr;
     double *acc = nullptr, *acc2 = nullptr;
+    unsigned *remaining = nullptr;  // exact subtractive rule: nodes still unresolved
 };
 
 void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, double lambda, bool extract,

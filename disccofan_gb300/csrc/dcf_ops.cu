@@ -113,6 +113,59 @@ __global__ void k_jump_sum(Geom g, const unsigned char *__restrict__ isroot, con
     }
 }
 
+// Subtractive rule with the reference's float arithmetic, for images whose levels
+// are not small integers: value(u) = (gval(u) + value(w)) - gval(w) for a surviving
+// node u under w, value(w) for a removed one, evaluated top-down in float as
+// filtering.c:231-243 does.  Each node walks up (at most SUB_STACK steps) to the
+// nearest ancestor whose value is known, then evaluates the walked path downward;
+// nodes further than that from any known value retry in the next launch.
+constexpr int SUB_STACK = 48;
+
+__global__ void k_sub_exact(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                            const float *__restrict__ gval, const unsigned char *__restrict__ flag, float *val,
+                            unsigned char *known, unsigned *remaining)
+{
+    unsigned left = 0;
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p] || ((volatile unsigned char *)known)[p]) continue;
+        int stk[SUB_STACK];
+        int n = 0, v = (int)p;
+        bool have = false, at_root = false;
+        while (n < SUB_STACK) {
+            if (((volatile unsigned char *)known)[v]) { have = true; break; }
+            stk[n++] = v;
+            int q = parent[v];
+            if (q == NONE) { at_root = true; break; }
+            v = q;
+        }
+        if (!have && !at_root) { left++; continue; }
+        __threadfence();  // pairs with the writer's fence between value and flag
+        int j = n - 1;
+        float above;
+        if (at_root) {  // stk[j] is the root
+            int r = stk[j];
+            above = flag[r] ? gval[r] : 0.0f;
+            ((volatile float *)val)[r] = above;
+            __threadfence();
+            ((volatile unsigned char *)known)[r] = 1;
+            j--;
+        } else {
+            above = ((volatile float *)val)[v];
+        }
+        for (; j >= 0; j--) {
+            int w = stk[j], pw = parent[w];
+            float f = flag[w] ? __fsub_rn(__fadd_rn(gval[w], above), gval[pw]) : above;
+            ((volatile float *)val)[w] = f;
+            __threadfence();
+            ((volatile unsigned char *)known)[w] = 1;
+            above = f;
+        }
+    }
+    for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
+    if ((threadIdx.x & 31) == 0 && left) atomicAdd(remaining, left);
+}
+
 // min rule: best(u) = topmost removed node on u's path, root excluded
 __global__ void k_min_init(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
                            const unsigned char *__restrict__ flag, int *jump, int *best)
@@ -160,6 +213,8 @@ __global__ void k_filter_out(Geom g, const unsigned char *__restrict__ isroot, c
             val = s >= 0 ? gval[s] : 0.0f;
         } else if (RULE == 3) {
             val = (float)acc[node];
+        } else if (RULE == 4) {
+            val = ((const float *)acc)[node];
         } else {  // min
             int r = target[node];
             if (r != NONE) val = gval[parent[r]];
@@ -195,7 +250,22 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     } else {
         const int R = rounds_for(depth_bound);
         int *j0 = w.jump, *j1 = w.jump2;
-        if (rule == 3) {
+        if (rule == 3 && !t.integer_levels) {
+            // exact float recurrence, repeated until every node is resolved
+            float *val = (float *)w.acc;
+            unsigned char *known = (unsigned char *)w.acc2;
+            cudaMemsetAsync(known, 0, t.g.N, s);
+            for (long long launch = 0; launch <= t.g.N / SUB_STACK + 1; launch++) {
+                cudaMemsetAsync(w.remaining, 0, sizeof(unsigned), s);
+                k_sub_exact<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, val, known, w.remaining);
+                unsigned left = 0;
+                cudaMemcpyAsync(&left, w.remaining, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+                cudaStreamSynchronize(s);
+                if (left == 0) break;
+            }
+            accp = (const double *)val;
+            rule = 4;
+        } else if (rule == 3) {
             double *a0 = w.acc, *a1 = w.acc2;
             k_sub_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, j0, a0);
             for (int r = 0; r < R; r++) {
@@ -221,7 +291,8 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     case 0: DCF_OUT(0); break;
     case 1: DCF_OUT(1); break;
     case 2: DCF_OUT(2); break;
-    default: DCF_OUT(3); break;
+    case 3: DCF_OUT(3); break;
+    default: DCF_OUT(4); break;
     }
 #undef DCF_OUT
 }

@@ -15,6 +15,20 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 FLOAT_ATTR_RTOL = 1e-9
+# 3-D non-compactness divides by pow(area, 5.0/3.0); the device evaluates that power in
+# double-double and agrees with glibc's pow except where glibc is not correctly
+# rounded (~0.1% of values, 1 ulp)
+POW_RTOL = 4e-16
+
+
+def assert_attr(got, want, attr, exact, is3d):
+    if attr == 17 and is3d:
+        np.testing.assert_allclose(got, want, rtol=POW_RTOL if exact else FLOAT_ATTR_RTOL, atol=0, equal_nan=True,
+                                   err_msg=str(attr))
+    elif exact or attr < 9 or attr == 18:
+        assert np.array_equal(got, want, equal_nan=True), attr
+    else:
+        np.testing.assert_allclose(got, want, rtol=FLOAT_ATTR_RTOL, atol=1e-9, equal_nan=True, err_msg=str(attr))
 
 
 def gpu_tree(ctx, img, conn, tree="max", attr=0):
@@ -54,18 +68,14 @@ def test_synthetic_reference_outputs(ctx, synthetic, name):
     t = gpu_tree(ctx, img, int(c["conn"]), c["tree"].item().decode())
     assert np.array_equal(t.parent(), c["parent"])
     assert np.array_equal(t.node_attribute(0), c["area"], equal_nan=True)
-    for rule in (0, 3):
+    for rule in range(4):
         assert np.array_equal(t.filter(0, 12.0, rule), c[f"filter_area_r{rule}"]), rule
     assert np.array_equal(t.filter(0, 12.0, 0, extract=True), c["extract_area"])
     lv = dcf.lvec_from_values([2, 5, 10, 50, 200])
     assert np.array_equal(t.pattern_spectrum(0, lv), c["pattern_area"])
     exact = img.dtype != np.float32
     for a in range(1, 18):
-        got, want = t.node_attribute(a), c[f"attr{a}"]
-        if exact or a < 9:
-            assert np.array_equal(got, want, equal_nan=True), a
-        else:
-            np.testing.assert_allclose(got, want, rtol=FLOAT_ATTR_RTOL, atol=1e-12, equal_nan=True, err_msg=str(a))
+        assert_attr(t.node_attribute(a), c[f"attr{a}"], a, exact, img.ndim == 3)
     assert np.array_equal(t.filter(17, 0.3, 0), c["filter_ncomp_r0"])
     l1 = dcf.lvec_from_values([1.2, 2, 4])
     s2 = t.pattern_spectrum2d(14, l1, 0, lv)
@@ -104,7 +114,7 @@ def test_random_against_oracle(ctx, shape, kind, conn, tree):
     assert np.array_equal(t.parent(), port.parent())
     assert np.array_equal(t.gval(), port.gval())
     assert np.array_equal(t.node_attribute(0), port.node_attr(0), equal_nan=True)
-    for rule in (0, 3):
+    for rule in (0, 1, 2, 3):
         lam = 5.0
         assert np.array_equal(t.filter(0, lam, rule), port.filter(0, lam, rule)), rule
     lv = dcf.lvec_from_values([2, 4, 16, 64])
@@ -115,11 +125,7 @@ def test_random_against_oracle(ctx, shape, kind, conn, tree):
         assert np.array_equal(t.pattern_spectrum(0, lv), want)
     exact = kind in ("u8", "u16")
     for a in (1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 16, 17, 18):
-        got, want = t.node_attribute(a), port.node_attr(a)
-        if exact or a < 9 or a == 18:
-            assert np.array_equal(got, want, equal_nan=True), a
-        else:
-            np.testing.assert_allclose(got, want, rtol=FLOAT_ATTR_RTOL, atol=1e-9, equal_nan=True, err_msg=str(a))
+        assert_attr(t.node_attribute(a), port.node_attr(a), a, exact, len(shape) == 3)
 
 
 def test_constant_image_single_node(ctx):
