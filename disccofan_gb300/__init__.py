@@ -100,6 +100,13 @@ def library() -> C.CDLL:
     L.dcf_status_string.restype = C.c_char_p
     L.dcf_ctx_launch_count.argtypes = [vp]
     L.dcf_ctx_launch_count.restype = C.c_uint64
+    L.dcf_ctx_set_profiling.argtypes = [vp, i]
+    L.dcf_ctx_set_profiling.restype = C.c_int
+    L.dcf_ctx_profile.argtypes = [vp, i, C.POINTER(d), C.POINTER(u64)]
+    L.dcf_ctx_profile.restype = C.c_int
+    L.dcf_profile_num_kernels.restype = C.c_int
+    L.dcf_profile_kernel_name.argtypes = [i]
+    L.dcf_profile_kernel_name.restype = C.c_char_p
     _lib = L
     return L
 
@@ -164,6 +171,20 @@ class Context:
     @property
     def launches(self) -> int:
         return int(self.lib.dcf_ctx_launch_count(self.h))
+
+    def set_profiling(self, enable: bool = True):
+        """Per-kernel CUDA-event timing on this context's stream (resets totals)."""
+        self.check(self.lib.dcf_ctx_set_profiling(self.h, int(enable)), "set_profiling")
+
+    def profile(self) -> dict:
+        """{kernel name: (total device ms, launch groups)} since profiling was enabled."""
+        out = {}
+        for k in range(self.lib.dcf_profile_num_kernels()):
+            ms, n = C.c_double(), C.c_uint64()
+            self.check(self.lib.dcf_ctx_profile(self.h, k, C.byref(ms), C.byref(n)), "profile")
+            if n.value:
+                out[self.lib.dcf_profile_kernel_name(k).decode()] = (ms.value, n.value)
+        return out
 
     def build(self, image, connectivity: int = 4, tree_type: str = "max", attribute: int = 0,
               pixdim=(1.0, 1.0, 1.0)) -> "Tree":
@@ -244,7 +265,8 @@ class Tree:
         self.attribute = attribute
 
     def _ensure_group(self, attribute: int):
-        if ATTR_GROUP[attribute] != ATTR_GROUP[self.attribute]:
+        # area (0) is readable from every group's records
+        if attribute != 0 and ATTR_GROUP[attribute] != ATTR_GROUP[self.attribute]:
             self.set_attribute(attribute)
 
     def info(self):

@@ -19,6 +19,12 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+struct ProfEvent {
+    cudaEvent_t ev;
+    int id;
+    bool begin;
+};
+
 struct dcf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -29,10 +35,69 @@ struct dcf_ctx {
     char last_error[512] = {0};
     uint64_t launches = 0;
     DevBuf scratch[8];                // reusable work buffers (filter, spectra)
+    bool prof_on = false;
+    ProfEvent *prof_ev = nullptr;     // recorded events, in launch order
+    int prof_n = 0, prof_cap = 0;
+    double prof_ms[P_COUNT] = {0};
+    uint64_t prof_cnt[P_COUNT] = {0};
 };
+
+// the context whose API call is running on this thread (for prof_begin/prof_end)
+static thread_local dcf_ctx *t_active = nullptr;
+struct ActiveScope {
+    dcf_ctx *prev;
+    explicit ActiveScope(dcf_ctx *c) : prev(t_active) { t_active = c; }
+    ~ActiveScope() { t_active = prev; }
+};
+
+static void prof_record(int id, bool begin, cudaStream_t s)
+{
+    dcf_ctx *c = t_active;
+    if (!c || !c->prof_on) return;
+    if (c->prof_n == c->prof_cap) {
+        int cap = c->prof_cap ? 2 * c->prof_cap : 256;
+        ProfEvent *nv = (ProfEvent *)realloc(c->prof_ev, cap * sizeof(ProfEvent));
+        if (!nv) return;
+        for (int i = c->prof_cap; i < cap; i++) cudaEventCreate(&nv[i].ev);
+        c->prof_ev = nv;
+        c->prof_cap = cap;
+    }
+    ProfEvent &e = c->prof_ev[c->prof_n++];
+    e.id = id;
+    e.begin = begin;
+    cudaEventRecord(e.ev, s);
+}
+
+namespace dcf {
+void prof_begin(int id, cudaStream_t s) { prof_record(id, true, s); }
+void prof_end(int id, cudaStream_t s) { prof_record(id, false, s); }
+}  // namespace dcf
+
+// fold recorded event pairs into per-kernel totals
+static void prof_collect(dcf_ctx *c)
+{
+    if (!c->prof_n) return;
+    cudaStreamSynchronize(c->stream);
+    int open[P_COUNT];
+    for (int i = 0; i < P_COUNT; i++) open[i] = -1;
+    for (int i = 0; i < c->prof_n; i++) {
+        ProfEvent &e = c->prof_ev[i];
+        if (e.begin) {
+            open[e.id] = i;
+        } else if (open[e.id] >= 0) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, c->prof_ev[open[e.id]].ev, e.ev);
+            c->prof_ms[e.id] += ms;
+            c->prof_cnt[e.id]++;
+            open[e.id] = -1;
+        }
+    }
+    c->prof_n = 0;
+}
 
 struct dcf_tree {
     dcf_ctx *ctx = nullptr;
+    cudaStream_t stream = nullptr;           // buffers are freed in this stream's order
     Geom g{};
     int dtype = 0;
     bool tree_min = false;
@@ -143,6 +208,13 @@ dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out)
         ctx->own_stream = true;
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    // keep freed tree buffers in the device's default pool: repeated builds then
+    // allocate stream-ordered without cudaMalloc's cost or its implicit sync
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (cudaMalloc(&ctx->d_err, 4 * sizeof(unsigned)) != cudaSuccess ||
         cudaMemset(ctx->d_err, 0, 4 * sizeof(unsigned)) != cudaSuccess) {
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -159,6 +231,8 @@ dcf_status dcf_ctx_destroy(dcf_ctx *ctx)
     cudaStreamSynchronize(ctx->stream);
     for (auto &b : ctx->scratch)
         if (b.p) cudaFree(b.p);
+    for (int i = 0; i < ctx->prof_cap; i++) cudaEventDestroy(ctx->prof_ev[i].ev);
+    free(ctx->prof_ev);
     cudaFree(ctx->d_err);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -175,9 +249,40 @@ const char *dcf_ctx_last_error(const dcf_ctx *ctx) { return ctx ? ctx->last_erro
 
 uint64_t dcf_ctx_launch_count(const dcf_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+dcf_status dcf_ctx_set_profiling(dcf_ctx *ctx, int enable)
+{
+    if (!ctx) return DCF_ERR_INVALID;
+    prof_collect(ctx);
+    ctx->prof_on = enable != 0;
+    for (int i = 0; i < P_COUNT; i++) {
+        ctx->prof_ms[i] = 0.0;
+        ctx->prof_cnt[i] = 0;
+    }
+    return DCF_OK;
+}
+
+int dcf_profile_num_kernels(void) { return P_COUNT; }
+
+const char *dcf_profile_kernel_name(int id)
+{
+    static const char *names[P_COUNT] = {"stats", "tile_build", "seam_merge", "canonicalise", "attr_pixels",
+                                         "attr_bottom_up", "filter_flag", "filter_resolve", "filter_jump",
+                                         "filter_out", "check", "spectrum", "copy", "batch", "adjoint"};
+    return (id >= 0 && id < P_COUNT) ? names[id] : "?";
+}
+
+dcf_status dcf_ctx_profile(dcf_ctx *ctx, int id, double *total_ms, uint64_t *launches)
+{
+    if (!ctx || id < 0 || id >= P_COUNT) return DCF_ERR_INVALID;
+    prof_collect(ctx);
+    if (total_ms) *total_ms = ctx->prof_ms[id];
+    if (launches) *launches = ctx->prof_cnt[id];
+    return DCF_OK;
+}
+
 static void free_attr(dcf_tree *t)
 {
-    if (t->attr_mem) cudaFree(t->attr_mem);
+    if (t->attr_mem) cudaFreeAsync(t->attr_mem, t->stream);
     t->attr_mem = nullptr;
     t->attr = AttrBufs();
     t->attr_idx = -1;
@@ -186,12 +291,13 @@ static void free_attr(dcf_tree *t)
 dcf_status dcf_tree_destroy(dcf_tree *t)
 {
     if (!t) return DCF_ERR_INVALID;
-    // cudaFree waits for the device; the context (and its stream) may already be gone
+    // stream-ordered frees: the memory returns to the pool once queued work is done.
+    // Trees must be destroyed before their context.
     free_attr(t);
-    cudaFree(t->gval);
-    cudaFree(t->parent);
-    cudaFree(t->isroot);
-    cudaFree(t->stats);
+    if (t->gval) cudaFreeAsync(t->gval, t->stream);
+    if (t->parent) cudaFreeAsync(t->parent, t->stream);
+    if (t->isroot) cudaFreeAsync(t->isroot, t->stream);
+    if (t->stats) cudaFreeAsync(t->stats, t->stream);
     delete t;
     return DCF_OK;
 }
@@ -223,7 +329,7 @@ static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
     const size_t n32 = 1 + 1 + (group == 1 ? 6 : 0);                                  // area, pending, bbox
     const size_t n64 = (group == 2 ? 3 : 0) + (group == 3 ? 5 : 0) + (group == 4 ? 14 : 0);
     const size_t bytes = (n32 * 4 + n64 * 8) * N + 256;
-    CU(cudaMalloc(&t->attr_mem, bytes));
+    CU(cudaMallocAsync(&t->attr_mem, bytes, ctx->stream));
     char *m = (char *)t->attr_mem;
     AttrBufs &a = t->attr;
     a.group = group;
@@ -253,6 +359,7 @@ static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
 
 dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_tree **out)
 {
+    ActiveScope active_scope_(ctx);
     if (!ctx || !img || !out) return DCF_ERR_INVALID;
     *out = nullptr;
     if (!img->data) return set_err(ctx, DCF_ERR_INVALID, "null image data");
@@ -279,6 +386,7 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
     dcf_tree *t = new (std::nothrow) dcf_tree();
     if (!t) return DCF_ERR_NOMEM;
     t->ctx = ctx;
+    t->stream = ctx->stream;
     t->g.W = (int)W;
     t->g.H = (int)H;
     t->g.D = (int)D;
@@ -303,10 +411,10 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
             goto fail;                  \
         }                               \
     } while (0)
-    TRY(cudaMalloc(&t->gval, N * sizeof(float)));
-    TRY(cudaMalloc(&t->parent, N * sizeof(int)));
-    TRY(cudaMalloc(&t->isroot, N));
-    TRY(cudaMalloc(&t->stats, 4 * sizeof(unsigned) + sizeof(unsigned long long)));
+    TRY(cudaMallocAsync(&t->gval, N * sizeof(float), ctx->stream));
+    TRY(cudaMallocAsync(&t->parent, N * sizeof(int), ctx->stream));
+    TRY(cudaMallocAsync(&t->isroot, N, ctx->stream));
+    TRY(cudaMallocAsync(&t->stats, 4 * sizeof(unsigned) + sizeof(unsigned long long), ctx->stream));
     t->num_nodes = (unsigned long long *)(t->stats + 4);
     if (!img->on_device) {
         TRY(cudaMallocAsync(&tmp_in, in_bytes, ctx->stream));
@@ -353,6 +461,7 @@ fail:
 
 dcf_status dcf_tree_set_attribute(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
 {
+    ActiveScope active_scope_(ctx);
     if (!ctx || !t) return DCF_ERR_INVALID;
     if (attr_idx < 0 || attr_idx >= DCF_NUM_ATTRIBUTES) return set_err(ctx, DCF_ERR_INVALID, "bad attribute");
     return compute_attributes(ctx, t, attr_idx);
@@ -412,6 +521,7 @@ __global__ void k_widen(long long n, const int *__restrict__ in, long long *out)
 
 dcf_status dcf_tree_parent(dcf_ctx *ctx, dcf_tree *t, int64_t *parent, int on_device)
 {
+    ActiveScope active_scope_(ctx);
     if (!ctx || !t || !parent) return DCF_ERR_INVALID;
     const size_t N = (size_t)t->g.N;
     long long *dst = (long long *)parent;
@@ -444,7 +554,8 @@ static dcf_status check_attr(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
 {
     if (attr_idx < 0 || attr_idx >= DCF_NUM_ATTRIBUTES) return set_err(ctx, DCF_ERR_INVALID, "bad attribute %d", attr_idx);
     if (!t->attr_mem) return set_err(ctx, DCF_ERR_STATE, "tree has no attributes");
-    if (ATTR_GROUP[attr_idx] != t->attr.group)
+    // attribute 0 (area) reads the area count every group's record carries
+    if (attr_idx != 0 && ATTR_GROUP[attr_idx] != t->attr.group)
         return set_err(ctx, DCF_ERR_STATE, "attribute %d is not in the tree's group %d (use dcf_tree_set_attribute)",
                        attr_idx, t->attr.group);
     return DCF_OK;
@@ -452,6 +563,7 @@ static dcf_status check_attr(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
 
 dcf_status dcf_node_attribute(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int area, double *out, int on_device)
 {
+    ActiveScope active_scope_(ctx);
     if (!ctx || !t || !out) return DCF_ERR_INVALID;
     dcf_status st = check_attr(ctx, t, attr_idx);
     if (st != DCF_OK) return st;
@@ -521,6 +633,7 @@ static dcf_status run_filter(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, 
 dcf_status dcf_filter(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, double lambda, int extract, float *out,
                       int on_device)
 {
+    ActiveScope active_scope_(ctx);
     if (!ctx || !t || !out) return DCF_ERR_INVALID;
     if (rule < 0 || rule > 3) return set_err(ctx, DCF_ERR_INVALID, "bad rule %d", rule);
     dcf_status st = check_attr(ctx, t, attr_idx);
@@ -558,6 +671,7 @@ dcf_status dcf_dmp(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, const floa
 
 dcf_status dcf_attribute_check(dcf_ctx *ctx, dcf_tree *t, int attr_idx, float *out, int on_device)
 {
+    ActiveScope active_scope_(ctx);
     if (!ctx || !t || !out) return DCF_ERR_INVALID;
     dcf_status st = check_attr(ctx, t, attr_idx);
     if (st != DCF_OK) return st;
@@ -583,6 +697,7 @@ dcf_status dcf_attribute_check(dcf_ctx *ctx, dcf_tree *t, int attr_idx, float *o
 static dcf_status spectrum_common(dcf_ctx *ctx, dcf_tree *t, int a1, const float *l1, int n1, int a2,
                                   const float *l2, int n2, double *spec, int on_device)
 {
+    ActiveScope active_scope_(ctx);
     if (n1 < 1 || n2 < 1 || !l1 || !l2 || !spec) return set_err(ctx, DCF_ERR_INVALID, "bad lambda vectors");
     const size_t nb = (size_t)n1 * n2;
     void *s;

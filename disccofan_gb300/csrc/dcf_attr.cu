@@ -25,18 +25,20 @@ template <int G, bool EXACT>
 __global__ void k_attr_pixels(const float *__restrict__ gval, Geom g, const int *__restrict__ parent,
                               const unsigned char *__restrict__ isroot, AttrBufs a)
 {
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
-         p += (long long)gridDim.x * blockDim.x) {
-        const int par = parent[p];
-        const bool root = isroot[p];
-        const int node = root ? (int)p : par;
+    // whole warps iterate together (uniform trip count), so the match below always
+    // has the full warp: the area of lanes in one flat zone is added once
+    const int lane = threadIdx.x & 31;
+    const long long wstride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (blockIdx.x * (long long)blockDim.x + threadIdx.x) - lane; base < g.N; base += wstride) {
+        const long long p = base + lane;
+        const bool valid = p < g.N;
+        const int par = valid ? parent[p] : NONE;
+        const bool root = valid && isroot[p];
+        const int node = valid ? (root ? (int)p : par) : -2;
         if (root && par != NONE) atomicAdd(a.pending + par, 1);
-        // warp-aggregated area
-        unsigned act = __activemask();
-        unsigned grp = __match_any_sync(act, node);
-        int lane = threadIdx.x & 31;
-        if (lane == __ffs(grp) - 1) atomicAdd(a.area + node, (unsigned)__popc(grp));
-        if (G == 0) continue;
+        unsigned grp = __match_any_sync(0xffffffffu, node);
+        if (valid && lane == __ffs(grp) - 1) atomicAdd(a.area + node, (unsigned)__popc(grp));
+        if (G == 0 || !valid) continue;
         const unsigned x = (unsigned)(p % g.W), y = (unsigned)((p / g.W) % g.H), z = (unsigned)(p / g.WH);
         if (G == 1) {
             atomicMin(a.bmin[0] + node, x);
@@ -139,6 +141,7 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm, cu
 {
     int nb = grid_for(t.g.N, 256, sm);
 #define DCF_PIX(G, E) k_attr_pixels<G, E><<<nb, 256, 0, s>>>(t.gval, t.g, t.parent, t.isroot, a)
+    prof_begin(P_ATTR_PIX, s);
     switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
     case 0: case 1: DCF_PIX(0, false); break;
     case 2: case 3: DCF_PIX(1, false); break;
@@ -149,6 +152,8 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm, cu
     default: DCF_PIX(4, true); break;
     }
 #undef DCF_PIX
+    prof_end(P_ATTR_PIX, s);
+    prof_begin(P_ATTR_UP, s);
     k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending);
 #define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, err)
     switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
@@ -161,6 +166,7 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm, cu
     default: DCF_UP(4, true); break;
     }
 #undef DCF_UP
+    prof_end(P_ATTR_UP, s);
 }
 
 __global__ void k_node_attr(Geom g, const unsigned char *__restrict__ isroot, AttrBufs a, int attr, bool area,

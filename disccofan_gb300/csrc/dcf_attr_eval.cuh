@@ -109,8 +109,8 @@ __device__ __forceinline__ void inertia_arr(const AttrBufs &a, int u, const floa
 __device__ __forceinline__ double attr_value(const AttrBufs &a, int attr, int u, const float *pd)
 {
     switch (attr) {
-    case 0:
-        return area_value(a, u, pd);
+    case 0: /* area_attribute (attributes.c:105); every group's record has the area count */
+        return (double)__fmul_rn(__fmul_rn(__fmul_rn(pd[0], pd[1]), pd[2]), __uint2float_rn(a.area[u]));
     case 1: { /* extent_rectarea_attribute (attributes.c:218) */
         double v = (double)(a.bmax[0][u] - a.bmin[0][u]) * (double)(a.bmax[1][u] - a.bmin[1][u]) *
                    (double)(a.bmax[2][u] - a.bmin[2][u]);

@@ -135,6 +135,10 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
         for (int half = 1; half < ext; half <<= 1) {
             const int nseams = (ext + 2 * half - 1) / (2 * half);
             const int other = axis == 1 ? TD : TH;  // slices (axis y) or rows (axis z)
+            // all edges across the seams of this level at once; correctness does not
+            // depend on the order (see connect), and for the deep chains of high
+            // dynamic-range tiles concurrent walkers finish sooner than any ordering
+            // by fewer threads
             const long long work = (long long)nseams * other * TW;
             for (long long w = tid; w < work; w += TILE_THREADS) {
                 int lx = (int)(w % TW);
@@ -154,7 +158,6 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
                     if (!crosses) continue;
                     int qx = lx - dx, qy = ly - dy, qz = lz - dz;
                     if (qx < 0 || qx >= wl || qy < 0 || qy >= hl || qz < 0 || qz >= dl) continue;
-                    if (axis == 2 && (qy < 0 || qy >= hl)) continue;
                     connect(acc, p, qx + qy * TW + qz * TW * TH, MERGE_BOUND_SMEM);
                 }
             }
@@ -206,26 +209,59 @@ struct GlobalAcc {
     __device__ void error(unsigned bit) { raise_error(err, bit); }
 };
 
-// One thread per pixel on a tile's shell; every forward edge that leaves the tile
-// is merged.  Each cross-tile edge has exactly one low endpoint, so none repeats.
-__global__ void k_seam_merge(const float *__restrict__ gval, Geom g, int *parent, unsigned *err)
+// Seam merge: work item = (tile, face, segment).  Faces are the tile's +x, -x, +y,
+// -y, +z sides (forward offsets never point to -z); a segment is a run of face
+// pixels one thread walks in order, merging every forward edge of each pixel that
+// leaves the tile.  Every cross-tile edge leaves its low endpoint's tile through
+// one of these faces, so all are merged (edges at tile corners possibly twice,
+// which is harmless); in-order processing keeps the merge walks short, as inside
+// the tile.
+constexpr int SEAM_SEG = 16;
+
+// largest face (2-D: a 64-pixel side; 3-D: a 16x16 face) in SEAM_SEG runs
+__host__ __device__ inline int seam_segments_per_face(bool is3d) { return is3d ? 256 / SEAM_SEG : 64 / SEAM_SEG; }
+
+__global__ void k_seam_merge(const float *__restrict__ gval, Geom g, int ntx, int nty, int ntz, int *parent,
+                             unsigned *err)
 {
     const bool is3d = g.D > 1;
     const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
     GlobalAcc acc{gval, parent, err, g.N};
     const Offs offs = forward_offsets(g.conn);
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
-         p += (long long)gridDim.x * blockDim.x) {
-        int x = (int)(p % g.W), y = (int)((p / g.W) % g.H), z = (int)(p / g.WH);
-        int lx = x % TW, ly = y % TH, lz = z % TD;
-        bool shell = lx == 0 || lx == TW - 1 || ly == 0 || ly == TH - 1 || (is3d && (lz == 0 || lz == TD - 1));
-        if (!shell) continue;
-        for (int e = 0; e < offs.n; e++) {
-            int qx = x + offs.d[e][0], qy = y + offs.d[e][1], qz = z + offs.d[e][2];
-            if (qx < 0 || qx >= g.W || qy < 0 || qy >= g.H || qz >= g.D) continue;
-            if (qx / TW == x / TW && qy / TH == y / TH && qz / TD == z / TD) continue;
-            int q = (int)((long long)qz * g.WH + (long long)qy * g.W + qx);
-            connect(acc, (int)p, q, MERGE_BOUND_GLOBAL);
+    bool neg_x = false, neg_y = false;
+    for (int e = 0; e < offs.n; e++) {
+        neg_x |= offs.d[e][0] < 0;
+        neg_y |= offs.d[e][1] < 0;
+    }
+    // face f: 0 +x, 1 -x, 2 +y, 3 -y, 4 +z; pixels per face and segments per face
+    const int fpix[5] = {TH * TD, TH * TD, TW * TD, TW * TD, TW * TH};
+    const int nseg_face = seam_segments_per_face(is3d);
+    const long long ntiles = (long long)ntx * nty * ntz;
+    const long long work = ntiles * 5 * nseg_face;
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
+         w += (long long)gridDim.x * blockDim.x) {
+        const int sg = (int)(w % nseg_face);
+        const int f = (int)((w / nseg_face) % 5);
+        const long long tile = w / (5LL * nseg_face);
+        if ((f == 1 && !neg_x) || (f == 3 && !neg_y) || (f == 4 && !is3d)) continue;
+        if (sg * SEAM_SEG >= fpix[f]) continue;
+        const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
+        const int x0 = tx * TW, y0 = ty * TH, z0 = tz * TD;
+        const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
+        for (int k = sg * SEAM_SEG; k < min(fpix[f], (sg + 1) * SEAM_SEG); k++) {
+            int lx, ly, lz;
+            if (f <= 1) { lx = f == 0 ? wl - 1 : 0; ly = k % TH; lz = k / TH; }
+            else if (f <= 3) { ly = f == 2 ? hl - 1 : 0; lx = k % TW; lz = k / TW; }
+            else { lz = dl - 1; lx = k % TW; ly = k / TW; }
+            if (lx >= wl || ly >= hl || lz >= dl) continue;
+            const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+            const int p = (int)((long long)z * g.WH + (long long)y * g.W + x);
+            for (int e = 0; e < offs.n; e++) {
+                int qx = x + offs.d[e][0], qy = y + offs.d[e][1], qz = z + offs.d[e][2];
+                if (qx < 0 || qx >= g.W || qy < 0 || qy >= g.H || qz >= g.D) continue;
+                if (qx >= x0 && qx < x0 + TW && qy >= y0 && qy < y0 + TH && qz >= z0 && qz < z0 + TD) continue;
+                connect(acc, p, (int)((long long)qz * g.WH + (long long)qy * g.W + qx), MERGE_BOUND_GLOBAL);
+            }
         }
     }
 }
@@ -276,23 +312,36 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
     const bool is3d = a.g.D > 1;
     const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
     dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
+    prof_begin(P_TILE, s);
     k_tile_build<T, MIN><<<grid, TILE_THREADS, 0, s>>>(img, a.g, a.kmax, a.gval, a.parent, a.err);
+    prof_end(P_TILE, s);
     int nb = grid_for(a.g.N, 256, a.sm_count);
-    k_seam_merge<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.err);
+    prof_begin(P_SEAM, s);
+    {
+        const int nseg_face = seam_segments_per_face(is3d);
+        const long long work = (long long)grid.x * grid.y * grid.z * 5 * nseg_face;
+        k_seam_merge<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.gval, a.g, grid.x, grid.y, grid.z, a.parent,
+                                                                      a.err);
+    }
+    prof_end(P_SEAM, s);
+    prof_begin(P_CANON, s);
     k_canon_pixels<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.err);
     k_canon_roots<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.isroot, a.num_nodes, a.err);
+    prof_end(P_CANON, s);
 }
 
 void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsigned *kmax, unsigned *nans,
                   int sm_count, cudaStream_t s)
 {
     int nb = grid_for(n, 256, sm_count);
+    prof_begin(P_STATS, s);
     switch (dtype) {
     case U8: k_stats<uint8_t><<<nb, 256, 0, s>>>((const uint8_t *)img, n, kmin, kmax, nans); break;
     case U16: k_stats<uint16_t><<<nb, 256, 0, s>>>((const uint16_t *)img, n, kmin, kmax, nans); break;
     case U32: k_stats<uint32_t><<<nb, 256, 0, s>>>((const uint32_t *)img, n, kmin, kmax, nans); break;
     default: k_stats<float><<<nb, 256, 0, s>>>((const float *)img, n, kmin, kmax, nans); break;
     }
+    prof_end(P_STATS, s);
 }
 
 void launch_build(const BuildArgs &a, cudaStream_t s)

@@ -4,6 +4,16 @@
 
 namespace dcf {
 
+// Per-kernel timing: launchers bracket each kernel group with prof_begin/prof_end,
+// which record CUDA events on the launching stream when the calling context has
+// profiling switched on (dcf_ctx_set_profiling); otherwise they do nothing.
+enum ProfId : int {
+    P_STATS = 0, P_TILE, P_SEAM, P_CANON, P_ATTR_PIX, P_ATTR_UP, P_FLAG, P_RESOLVE, P_JUMP, P_FILTER_OUT,
+    P_CHECK, P_SPECTRUM, P_COPY, P_BATCH, P_ADJOINT, P_COUNT
+};
+void prof_begin(int id, cudaStream_t s);
+void prof_end(int id, cudaStream_t s);
+
 constexpr int TILE_THREADS = 256;
 constexpr int TILE_PIX = 4096;                 // 64x64 (2-D) or 16x16x16 (3-D)
 constexpr long long MERGE_BOUND_SMEM = 1LL << 22;

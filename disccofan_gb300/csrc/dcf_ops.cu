@@ -238,8 +238,11 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
                    float *out, const FilterWork &w, long long depth_bound, unsigned *err, int sm, cudaStream_t s)
 {
     const int nb = grid_for(t.g.N, 256, sm);
+    prof_begin(P_FLAG, s);
     k_flag<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
                               w.target);
+    prof_end(P_FLAG, s);
+    prof_begin(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
     const double *accp = nullptr;
     if (rule == 0) {
         k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err);
@@ -285,6 +288,8 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
             if (b0 != w.target) cudaMemcpyAsync(w.target, b0, t.g.N * sizeof(int), cudaMemcpyDeviceToDevice, s);
         }
     }
+    prof_end(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
+    prof_begin(P_FILTER_OUT, s);
 #define DCF_OUT(R) \
     k_filter_out<R><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, w.target, accp, extract, t.tree_min, t.kmax, out)
     switch (rule) {
@@ -295,6 +300,7 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     default: DCF_OUT(4); break;
     }
 #undef DCF_OUT
+    prof_end(P_FILTER_OUT, s);
 }
 
 __global__ void k_check(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent, AttrBufs a,
@@ -311,7 +317,9 @@ __global__ void k_check(Geom g, const unsigned char *__restrict__ isroot, const 
 void launch_check(const TreeView &t, const AttrBufs &a, int attr, float *out, int sm, cudaStream_t s)
 {
     const int nb = grid_for(t.g.N, 256, sm);
+    prof_begin(P_CHECK, s);
     k_check<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, a, attr, t.pixdim[0], t.pixdim[1], t.pixdim[2], out);
+    prof_end(P_CHECK, s);
 }
 
 // find_scale (pattern.c:7-24): the last bin whose lambda is <= the attribute
@@ -365,8 +373,10 @@ void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *
                      int n2, double *spec, int sm, cudaStream_t s)
 {
     const int nb = grid_for(t.g.N, 256, sm);
+    prof_begin(P_SPECTRUM, s);
     k_spectrum<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
                                   t.pixdim[1], t.pixdim[2], spec);
+    prof_end(P_SPECTRUM, s);
 }
 
 }  // namespace dcf

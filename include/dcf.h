@@ -85,6 +85,14 @@ const char *dcf_status_string(dcf_status s);
 /* number of device kernel launches issued through this context so far */
 uint64_t dcf_ctx_launch_count(const dcf_ctx *ctx);
 
+/* Per-kernel timing with CUDA events on the context's stream (0 = off).  Turning
+ * it on or off resets the totals; dcf_ctx_profile returns the summed device time
+ * and launch-group count of kernel `id` (0 <= id < dcf_profile_num_kernels()). */
+dcf_status dcf_ctx_set_profiling(dcf_ctx *ctx, int enable);
+dcf_status dcf_ctx_profile(dcf_ctx *ctx, int id, double *total_ms, uint64_t *launches);
+int dcf_profile_num_kernels(void);
+const char *dcf_profile_kernel_name(int id);
+
 /* ---- tree ---- */
 /* Build the max-tree (min-tree: of the inverted image) with the attribute group
  * of attr_idx.  The image is copied to the device when on_device == 0. */
