@@ -263,6 +263,7 @@ def run_ours(args):
         "canonicalise": npix * (4 + 4 + 1),         # parent read+write, root flag
         "attr_pixels": npix * (4 + 1) + M * 12,     # parent + root flag in, area+bbox records out
         "attr_bottom_up": M * (12 + 4 + 4),         # records folded once, parent + counter per node
+        "attr_pointer_jump": M * (12 + 4),
         "filter_flag": M * 12 + npix * 1,
         "filter_resolve": M * (4 + 4),
         "filter_out": npix * (4 + 4 + 4),           # parent + target in, float image out

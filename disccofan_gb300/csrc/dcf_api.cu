@@ -6,7 +6,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <set>
 #include <string>
 
 #include "../../include/dcf.h"
@@ -34,7 +36,10 @@ struct dcf_ctx {
     unsigned *d_stats = nullptr;      // kmin, kmax, nans (per build; tree copies what it needs)
     char last_error[512] = {0};
     uint64_t launches = 0;
-    DevBuf scratch[8];                // reusable work buffers (filter, spectra)
+    int up_steps = 2048;              // bottom-up fold steps per walker before pointer jumping
+    std::mutex trees_mu;
+    std::set<dcf_tree *> trees;       // live trees; orphaned (stream cleared) when the context goes
+    DevBuf scratch[12];               // reusable work buffers (filter, spectra, attributes)
     bool prof_on = false;
     ProfEvent *prof_ev = nullptr;     // recorded events, in launch order
     int prof_n = 0, prof_cap = 0;
@@ -168,6 +173,20 @@ static dcf_status scratch(dcf_ctx *ctx, int slot, size_t bytes, void **out)
     return DCF_OK;
 }
 
+// stream-ordered free, or a synchronous one for a tree whose context is gone
+static void dev_free(void *p, cudaStream_t s)
+{
+    if (!p) return;
+    if (s) cudaFreeAsync(p, s);
+    else cudaFree(p);
+}
+
+static void orphan_tree(dcf_tree *t)
+{
+    t->ctx = nullptr;
+    t->stream = nullptr;
+}
+
 extern "C" {
 
 const char *dcf_status_string(dcf_status s)
@@ -208,6 +227,10 @@ dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out)
         ctx->own_stream = true;
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (const char *e = getenv("DCF_UP_STEPS")) {
+        int v = atoi(e);
+        if (v >= 0 && v < (1 << 20)) ctx->up_steps = v;
+    }
     // keep freed tree buffers in the device's default pool: repeated builds then
     // allocate stream-ordered without cudaMalloc's cost or its implicit sync
     cudaMemPool_t pool;
@@ -229,6 +252,12 @@ dcf_status dcf_ctx_destroy(dcf_ctx *ctx)
 {
     if (!ctx) return DCF_ERR_INVALID;
     cudaStreamSynchronize(ctx->stream);
+    {
+        // trees that outlive their context free their buffers synchronously later
+        std::lock_guard<std::mutex> lk(ctx->trees_mu);
+        for (dcf_tree *t : ctx->trees) orphan_tree(t);
+        ctx->trees.clear();
+    }
     for (auto &b : ctx->scratch)
         if (b.p) cudaFree(b.p);
     for (int i = 0; i < ctx->prof_cap; i++) cudaEventDestroy(ctx->prof_ev[i].ev);
@@ -266,7 +295,7 @@ int dcf_profile_num_kernels(void) { return P_COUNT; }
 const char *dcf_profile_kernel_name(int id)
 {
     static const char *names[P_COUNT] = {"stats", "tile_build", "seam_merge", "canonicalise", "attr_pixels",
-                                         "attr_bottom_up", "filter_flag", "filter_resolve", "filter_jump",
+                                         "attr_bottom_up", "attr_pointer_jump", "filter_flag", "filter_resolve", "filter_jump",
                                          "filter_out", "check", "spectrum", "copy", "batch", "adjoint"};
     return (id >= 0 && id < P_COUNT) ? names[id] : "?";
 }
@@ -282,7 +311,7 @@ dcf_status dcf_ctx_profile(dcf_ctx *ctx, int id, double *total_ms, uint64_t *lau
 
 static void free_attr(dcf_tree *t)
 {
-    if (t->attr_mem) cudaFreeAsync(t->attr_mem, t->stream);
+    dev_free(t->attr_mem, t->stream);
     t->attr_mem = nullptr;
     t->attr = AttrBufs();
     t->attr_idx = -1;
@@ -293,11 +322,15 @@ dcf_status dcf_tree_destroy(dcf_tree *t)
     if (!t) return DCF_ERR_INVALID;
     // stream-ordered frees: the memory returns to the pool once queued work is done.
     // Trees must be destroyed before their context.
+    if (t->ctx) {
+        std::lock_guard<std::mutex> lk(t->ctx->trees_mu);
+        t->ctx->trees.erase(t);
+    }
     free_attr(t);
-    if (t->gval) cudaFreeAsync(t->gval, t->stream);
-    if (t->parent) cudaFreeAsync(t->parent, t->stream);
-    if (t->isroot) cudaFreeAsync(t->isroot, t->stream);
-    if (t->stats) cudaFreeAsync(t->stats, t->stream);
+    dev_free(t->gval, t->stream);
+    dev_free(t->parent, t->stream);
+    dev_free(t->isroot, t->stream);
+    dev_free(t->stats, t->stream);
     delete t;
     return DCF_OK;
 }
@@ -351,10 +384,28 @@ static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
     }
     // zero everything, then bbox minima to all-ones
     CU(cudaMemsetAsync(t->attr_mem, 0, (size_t)(m - (char *)t->attr_mem), ctx->stream));
-    if (group == 1) CU(cudaMemsetAsync(a.bmin[0], 0xFF, 3 * 4 * N, ctx->stream));
-    launch_attributes(view_of(t), a, ctx->d_err, ctx->sm_count, ctx->stream);
+    a.has_z = t->g.D > 1;
+    if (group == 1) {
+        CU(cudaMemsetAsync(a.bmin[0], 0xFF, (a.has_z ? 3 : 2) * 4 * N, ctx->stream));
+        if (!a.has_z) launch_fill_u32((long long)N, a.bmax[2], 1u, ctx->sm_count, ctx->stream);
+    }
+    unsigned *count = ctx->d_err + 2;
+    launch_attributes(view_of(t), a, count, ctx->up_steps, ctx->d_err, ctx->sm_count, ctx->stream);
+    dcf_status st = check_launch(ctx, 4);
+    if (st != DCF_OK) return st;
+    unsigned R = 0;
+    CU(cudaMemcpyAsync(&R, count, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (R > 0) {
+        void *ws;
+        st = scratch(ctx, 8, attr_rest_bytes(group, R), &ws);
+        if (st != DCF_OK) return st;
+        launch_attributes_rest(view_of(t), a, R, count, ws, ctx->d_err, ctx->sm_count, ctx->stream);
+        st = check_launch(ctx, 4);
+        if (st != DCF_OK) return st;
+    }
     t->attr_idx = attr_idx;
-    return check_launch(ctx, 3);
+    return DCF_OK;
 }
 
 dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_tree **out)
@@ -450,6 +501,10 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
     }
     st = compute_attributes(ctx, t, attr_idx);
     if (st != DCF_OK) goto fail;
+    {
+        std::lock_guard<std::mutex> lk(ctx->trees_mu);
+        ctx->trees.insert(t);
+    }
     *out = t;
     return DCF_OK;
 fail:

@@ -43,10 +43,12 @@ __global__ void k_attr_pixels(const float *__restrict__ gval, Geom g, const int 
         if (G == 1) {
             atomicMin(a.bmin[0] + node, x);
             atomicMin(a.bmin[1] + node, y);
-            atomicMin(a.bmin[2] + node, z);
             atomicMax(a.bmax[0] + node, x + 1);
             atomicMax(a.bmax[1] + node, y + 1);
-            atomicMax(a.bmax[2] + node, z + 1);
+            if (a.has_z) {
+                atomicMin(a.bmin[2] + node, z);
+                atomicMax(a.bmax[2] + node, z + 1);
+            }
             continue;
         }
         if (G == 2 || G == 4) {
@@ -83,6 +85,18 @@ __global__ void k_attr_pixels(const float *__restrict__ gval, Geom g, const int 
     }
 }
 
+// 2-D images: every pixel has z = 0, so the z extent of every node is [0, 1)
+__global__ void k_fill_u32(long long n, uint32_t *dst, uint32_t v)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = v;
+}
+
+void launch_fill_u32(long long n, uint32_t *dst, uint32_t v, int sm, cudaStream_t s)
+{
+    k_fill_u32<<<grid_for(n, 256, sm), 256, 0, s>>>(n, dst, v);
+}
+
 __global__ void k_mark_leaves(long long n, const unsigned char *__restrict__ isroot, int *pending)
 {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
@@ -95,7 +109,7 @@ __device__ __forceinline__ void fold_into(const AttrBufs &a, int u, int q)
 {
     atomicAdd(a.area + q, __ldcg(a.area + u));
     if (G == 1) {
-        for (int d = 0; d < 3; d++) {
+        for (int d = 0; d < (a.has_z ? 3 : 2); d++) {
             atomicMin(a.bmin[d] + q, __ldcg(a.bmin[d] + u));
             atomicMax(a.bmax[d] + q, __ldcg(a.bmax[d] + u));
         }
@@ -115,17 +129,26 @@ __device__ __forceinline__ void fold_into(const AttrBufs &a, int u, int q)
     }
 }
 
+constexpr int STALLED = -3;         // pending value of a complete node not folded upward
+
+// Bottom-up fold limited to up_steps nodes per walker: a walker stopping at a
+// complete node marks it STALLED instead of folding it into its parent.  What is
+// left (STALLED nodes and nodes still waiting for children) lies near the root and
+// is finished by pointer jumping (k_jump_fold).
 template <int G, bool EXACT>
-__global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs a, unsigned *err)
+__global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs a, int up_steps, unsigned *err)
 {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
          p += (long long)gridDim.x * blockDim.x) {
         if (__ldcg(a.pending + p) != -1) continue;
         int u = (int)p;
-        long long it = 0;
-        for (; it < n; it++) {
+        for (int step = 0;; step++) {
             int q = parent[u];
             if (q == NONE) break;
+            if (step == up_steps) {
+                a.pending[u] = STALLED;
+                break;
+            }
             fold_into<G, EXACT>(a, u, q);
             __threadfence();
             int before = atomicSub(a.pending + q, 1);
@@ -133,11 +156,164 @@ __global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs 
             __threadfence();
             u = q;
         }
-        if (it >= n) raise_error(err, DEVERR_WALK_BOUND);
     }
 }
 
-void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm, cudaStream_t s)
+// nodes left for the pointer-jumping phase, listed in any order
+__global__ void k_collect_rest(long long n, const unsigned char *__restrict__ isroot, int *pending, int *list,
+                               unsigned *count)
+{
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+         p += (long long)gridDim.x * blockDim.x) {
+        if (!isroot[p]) continue;
+        int s = pending[p];
+        if (s > 0 || s == STALLED) {
+            unsigned i = atomicAdd(count, 1u);
+            if (list) list[i] = (int)p;
+        }
+    }
+}
+
+// Compact records of the remaining nodes: R-long arrays, one per field.
+struct RestRecs {
+    uint32_t *area;
+    uint32_t *bmin[3], *bmax[3];
+    unsigned long long *s1[3], *s2[6];
+    void *gw[5];
+};
+
+template <int G>
+__device__ __forceinline__ void rest_copy(const RestRecs &dst, int i, const AttrBufs &src, int u, bool to_rest)
+{
+    if (to_rest) {
+        dst.area[i] = src.area[u];
+        if (G == 1) for (int d = 0; d < 3; d++) { dst.bmin[d][i] = src.bmin[d][u]; dst.bmax[d][i] = src.bmax[d][u]; }
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) dst.s1[d][i] = src.s1[d][u];
+        if (G == 4) for (int d = 0; d < 6; d++) dst.s2[d][i] = src.s2[d][u];
+        if (G == 3 || G == 4)
+            for (int d = 0; d < 5; d++) ((unsigned long long *)dst.gw[d])[i] = ((const unsigned long long *)src.gw[d])[u];
+    } else {
+        src.area[u] = dst.area[i];
+        if (G == 1) for (int d = 0; d < 3; d++) { src.bmin[d][u] = dst.bmin[d][i]; src.bmax[d][u] = dst.bmax[d][i]; }
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) src.s1[d][u] = dst.s1[d][i];
+        if (G == 4) for (int d = 0; d < 6; d++) src.s2[d][u] = dst.s2[d][i];
+        if (G == 3 || G == 4)
+            for (int d = 0; d < 5; d++) ((unsigned long long *)src.gw[d])[u] = ((const unsigned long long *)dst.gw[d])[i];
+    }
+}
+
+template <int G>
+__global__ void k_rest_gather(const int *__restrict__ list, const unsigned *count, const int *__restrict__ parent,
+                              int *pending, AttrBufs a, RestRecs r, int *jump, unsigned *err)
+{
+    const unsigned R = *count;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
+        rest_copy<G>(r, (int)i, a, list[i], true);
+        pending[list[i]] = -(int)(i + 16);  // position of the node in the compact list
+    }
+}
+
+template <int G>
+__global__ void k_rest_links(const int *__restrict__ list, const unsigned *count, const int *__restrict__ parent,
+                             const int *__restrict__ pending, int *jump, unsigned *err)
+{
+    const unsigned R = *count;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
+        int q = parent[list[i]];
+        int j = NONE;
+        if (q != NONE) {
+            int s = pending[q];
+            if (s <= -16) j = -s - 16;
+            else raise_error(err, DEVERR_WALK_BOUND);  // a parent of a remaining node must remain
+        }
+        jump[i] = j;
+    }
+}
+
+// One pointer-jumping round over the remaining forest: every node adds its partial
+// record into the node 2^k levels above it (sums; min/max for the bounding box).
+// Reads the `in` buffers, writes `out` (initialised as a copy of `in`).
+template <int G, bool EXACT>
+__global__ void k_jump_fold(const unsigned *count, const int *__restrict__ jin, int *jout, RestRecs in, RestRecs out,
+                            bool has_z)
+{
+    const unsigned R = *count;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
+        int j = jin[i];
+        if (j == NONE) {
+            jout[i] = NONE;
+            continue;
+        }
+        jout[i] = jin[j];
+        atomicAdd(out.area + j, in.area[i]);
+        if (G == 1)
+            for (int d = 0; d < (has_z ? 3 : 2); d++) {
+                atomicMin(out.bmin[d] + j, in.bmin[d][i]);
+                atomicMax(out.bmax[d] + j, in.bmax[d][i]);
+            }
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) atomicAdd(out.s1[d] + j, in.s1[d][i]);
+        if (G == 4) for (int d = 0; d < 6; d++) atomicAdd(out.s2[d] + j, in.s2[d][i]);
+        if (G == 3 || G == 4)
+            for (int d = 0; d < 5; d++) {
+                if (G == 3 && d == 1) continue;
+                if (EXACT) atomicAdd((unsigned long long *)out.gw[d] + j, ((const unsigned long long *)in.gw[d])[i]);
+                else atomicAdd((double *)out.gw[d] + j, ((const double *)in.gw[d])[i]);
+            }
+    }
+}
+
+template <int G>
+__global__ void k_rest_scatter(const int *__restrict__ list, const unsigned *count, AttrBufs a, RestRecs r)
+{
+    const unsigned R = *count;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x)
+        rest_copy<G>(r, (int)i, a, list[i], false);
+}
+
+static size_t rest_record_bytes(int group)
+{
+    size_t b = 4;
+    if (group == 1) b += 24;
+    if (group == 2) b += 24;
+    if (group == 3) b += 40;
+    if (group == 4) b += 24 + 48 + 40;
+    return b;
+}
+
+size_t attr_rest_bytes(int group, size_t R)
+{
+    // list + 2 jump arrays + 2 compact record buffers (each array 256-byte aligned)
+    return 3 * ((4 * R + 255) / 256 * 256) + 2 * (rest_record_bytes(group) * R + 16 * 256) + 256;
+}
+
+static RestRecs carve(char *&m, int group, size_t R)
+{
+    RestRecs r{};
+    auto take = [&](size_t bytes) { void *p = m; m += (bytes * R + 255) / 256 * 256; return p; };
+    r.area = (uint32_t *)take(4);
+    if (group == 1) for (int d = 0; d < 3; d++) { r.bmin[d] = (uint32_t *)take(4); r.bmax[d] = (uint32_t *)take(4); }
+    if (group == 2 || group == 4) for (int d = 0; d < 3; d++) r.s1[d] = (unsigned long long *)take(8);
+    if (group == 4) for (int d = 0; d < 6; d++) r.s2[d] = (unsigned long long *)take(8);
+    if (group == 3 || group == 4) for (int d = 0; d < 5; d++) r.gw[d] = take(8);
+    return r;
+}
+
+static void copy_recs(const RestRecs &dst, const RestRecs &src, int group, size_t R, cudaStream_t s)
+{
+    cudaMemcpyAsync(dst.area, src.area, 4 * R, cudaMemcpyDeviceToDevice, s);
+    for (int d = 0; d < 3; d++) {
+        if (dst.bmin[d]) cudaMemcpyAsync(dst.bmin[d], src.bmin[d], 4 * R, cudaMemcpyDeviceToDevice, s);
+        if (dst.bmax[d]) cudaMemcpyAsync(dst.bmax[d], src.bmax[d], 4 * R, cudaMemcpyDeviceToDevice, s);
+        if (dst.s1[d]) cudaMemcpyAsync(dst.s1[d], src.s1[d], 8 * R, cudaMemcpyDeviceToDevice, s);
+    }
+    for (int d = 0; d < 6; d++)
+        if (dst.s2[d]) cudaMemcpyAsync(dst.s2[d], src.s2[d], 8 * R, cudaMemcpyDeviceToDevice, s);
+    for (int d = 0; d < 5; d++)
+        if (dst.gw[d]) cudaMemcpyAsync(dst.gw[d], src.gw[d], 8 * R, cudaMemcpyDeviceToDevice, s);
+}
+
+void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_steps, unsigned *err, int sm,
+                       cudaStream_t s)
 {
     int nb = grid_for(t.g.N, 256, sm);
 #define DCF_PIX(G, E) k_attr_pixels<G, E><<<nb, 256, 0, s>>>(t.gval, t.g, t.parent, t.isroot, a)
@@ -155,7 +331,7 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm, cu
     prof_end(P_ATTR_PIX, s);
     prof_begin(P_ATTR_UP, s);
     k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending);
-#define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, err)
+#define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, up_steps, err)
     switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
     case 0: case 1: DCF_UP(0, false); break;
     case 2: case 3: DCF_UP(1, false); break;
@@ -166,7 +342,58 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm, cu
     default: DCF_UP(4, true); break;
     }
 #undef DCF_UP
+    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, nullptr, count);
     prof_end(P_ATTR_UP, s);
+}
+
+// Phase 2: R = number of nodes the walkers left (read back by the caller), scratch
+// = attr_rest_bytes(group, R) bytes.
+void launch_attributes_rest(const TreeView &t, AttrBufs &a, unsigned R, unsigned *count, void *scratch,
+                            unsigned *err, int sm, cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+    prof_begin(P_ATTR_REST, s);
+    char *m = (char *)scratch;
+    int *list = (int *)m;
+    m += (4 * (size_t)R + 255) / 256 * 256;
+    int *j0 = (int *)m;
+    m += (4 * (size_t)R + 255) / 256 * 256;
+    int *j1 = (int *)m;
+    m += (4 * (size_t)R + 255) / 256 * 256;
+    RestRecs r0 = carve(m, a.group, R), r1 = carve(m, a.group, R);
+    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, list, count);
+    if (R > 0) {
+        const int rb = grid_for(R, 256, sm);
+#define DCF_REST(G, E)                                                                           \
+    do {                                                                                         \
+        k_rest_gather<G><<<rb, 256, 0, s>>>(list, count, t.parent, a.pending, a, r0, j0, err);   \
+        k_rest_links<G><<<rb, 256, 0, s>>>(list, count, t.parent, a.pending, j0, err);          \
+        int rounds = 0;                                                                          \
+        while ((1u << rounds) < R && rounds < 31) rounds++;                                     \
+        RestRecs *ri = &r0, *ro = &r1;                                                           \
+        int *ji = j0, *jo = j1;                                                                  \
+        for (int k = 0; k < rounds; k++) {                                                       \
+            copy_recs(*ro, *ri, G, R, s);                                                        \
+            k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, ji, jo, *ri, *ro, a.has_z);                       \
+            RestRecs *tr = ri; ri = ro; ro = tr;                                                 \
+            int *tj = ji; ji = jo; jo = tj;                                                      \
+        }                                                                                        \
+        k_rest_scatter<G><<<rb, 256, 0, s>>>(list, count, a, *ri);                               \
+    } while (0)
+        switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
+        case 0: case 1: DCF_REST(0, false); break;
+        case 2: case 3: DCF_REST(1, false); break;
+        case 4: case 5: DCF_REST(2, false); break;
+        case 6: DCF_REST(3, false); break;
+        case 7: DCF_REST(3, true); break;
+        case 8: DCF_REST(4, false); break;
+        default: DCF_REST(4, true); break;
+        }
+#undef DCF_REST
+    }
+    prof_end(P_ATTR_REST, s);
 }
 
 __global__ void k_node_attr(Geom g, const unsigned char *__restrict__ isroot, AttrBufs a, int attr, bool area,

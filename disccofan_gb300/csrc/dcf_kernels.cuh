@@ -8,7 +8,7 @@ namespace dcf {
 // which record CUDA events on the launching stream when the calling context has
 // profiling switched on (dcf_ctx_set_profiling); otherwise they do nothing.
 enum ProfId : int {
-    P_STATS = 0, P_TILE, P_SEAM, P_CANON, P_ATTR_PIX, P_ATTR_UP, P_FLAG, P_RESOLVE, P_JUMP, P_FILTER_OUT,
+    P_STATS = 0, P_TILE, P_SEAM, P_CANON, P_ATTR_PIX, P_ATTR_UP, P_ATTR_REST, P_FLAG, P_RESOLVE, P_JUMP, P_FILTER_OUT,
     P_CHECK, P_SPECTRUM, P_COPY, P_BATCH, P_ADJOINT, P_COUNT
 };
 void prof_begin(int id, cudaStream_t s);
@@ -52,6 +52,7 @@ void launch_build(const BuildArgs &a, cudaStream_t s);
 struct AttrBufs {
     int group = -1;
     bool exact_g = false;            // grey-weighted sums kept as exact integers (u8/u16)
+    bool has_z = true;               // 3-D image: z extent is accumulated (2-D: fixed [0,1))
     uint32_t *area = nullptr;
     uint32_t *bmin[3] = {nullptr, nullptr, nullptr};
     uint32_t *bmax[3] = {nullptr, nullptr, nullptr};
@@ -72,7 +73,16 @@ struct TreeView {
     bool integer_levels;             // u8/u16 input: level arithmetic is exact in float
 };
 
-void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *err, int sm_count, cudaStream_t s);
+// Attribute accumulation in two launches: launch_attributes runs the pixel pass and
+// the bounded bottom-up fold and counts the nodes left into *count; the caller
+// reads that count R and calls launch_attributes_rest with attr_rest_bytes(group, R)
+// bytes of device scratch to finish them by pointer jumping.
+size_t attr_rest_bytes(int group, size_t R);
+void launch_fill_u32(long long n, uint32_t *dst, uint32_t v, int sm_count, cudaStream_t s);
+void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_steps, unsigned *err, int sm_count,
+                       cudaStream_t s);
+void launch_attributes_rest(const TreeView &t, AttrBufs &a, unsigned R, unsigned *count, void *scratch, unsigned *err,
+                            int sm_count, cudaStream_t s);
 
 // attribute readout of every level root into a double array (NaN elsewhere)
 void launch_node_attr(const TreeView &t, const AttrBufs &a, int attr, bool area, double *out, int sm_count,
