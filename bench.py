@@ -235,12 +235,12 @@ def run_ours(args):
 
     e2e_step()
     barrier()
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 5))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
     barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / max(e2e_steps, 1)
     h2d = 2 * npix * img.element_size()
     d2h = 2 * (npix * 4 + h_spec[0].nbytes)
 
@@ -371,6 +371,7 @@ def main():
     ap.add_argument("--size", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     args = ap.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
     if res is not None:
