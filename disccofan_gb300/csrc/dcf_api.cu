@@ -804,3 +804,58 @@ dcf_status dcf_pattern_spectrum2d(dcf_ctx *ctx, dcf_tree *t, int attr1, const fl
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free direct-rule filter.
+//
+// Some callers cannot allocate device memory at the moment they filter: a host
+// framework whose caching allocator has already reserved the device's free memory,
+// or a real-time loop that must never wait on, or fail in, an allocation.  For them
+// the per-pixel scratch of the direct rule (one survive byte and one resolved-node
+// index per pixel) lives in this fixed device array instead of the context's
+// buffers.  The array is NOALLOC_MAX_PIXELS * 5 bytes (40 MiB) and every GPU that
+// loads the library keeps it until the process exits.
+// ---------------------------------------------------------------------------
+static constexpr long long NOALLOC_MAX_PIXELS = 1LL << 23;  // 8,388,608 pixels
+static constexpr size_t NOALLOC_BYTES = (size_t)NOALLOC_MAX_PIXELS * 5 + 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[64];  // device address of g_noalloc_scratch, per device
+
+extern "C" dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *t, int attr_idx, double lambda,
+                                                int extract, float *out_device)
+{
+    if (!ctx || !t || !out_device) return DCF_ERR_INVALID;
+    if (t->g.N > NOALLOC_MAX_PIXELS)
+        return set_err(ctx, DCF_ERR_INVALID, "dcf_filter_direct_noalloc: %lld pixels exceed the fixed scratch of %lld",
+                       (long long)t->g.N, NOALLOC_MAX_PIXELS);
+    if (ctx->device < 0 || ctx->device >= 64) return set_err(ctx, DCF_ERR_INVALID, "device index out of range");
+    dcf_status st = check_attr(ctx, t, attr_idx);
+    if (st != DCF_OK) return st;
+    void *base = nullptr;
+    {
+        // one-time set-up per device, with that device current: the host-side
+        // name g_noalloc_scratch is not a device address, so look the address up
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[ctx->device]) {
+            CU(cudaSetDevice(ctx->device));
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p)
+                return set_err(ctx, DCF_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch): %s", cudaGetErrorString(e));
+            g_noalloc_ptr[ctx->device] = p;
+        }
+        base = g_noalloc_ptr[ctx->device];
+    }
+    ActiveScope active_scope_(ctx);
+    // layout: N resolved-node indices (int32), then N survive bytes; every call
+    // rewrites both for all pixels (k_flag resets the indices), so nothing carries
+    // over from the previous call
+    FilterWork w{};
+    w.target = (int *)base;
+    w.flag = (unsigned char *)base + (size_t)NOALLOC_MAX_PIXELS * 4;
+    launch_filter(view_of(t), t->attr, attr_idx, 0, lambda, extract != 0, out_device, w, depth_bound(t), ctx->d_err,
+                  ctx->sm_count, ctx->stream);
+    return check_launch(ctx, 3);
+}

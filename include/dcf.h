@@ -135,6 +135,20 @@ dcf_status dcf_pattern_spectrum(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, cons
 dcf_status dcf_pattern_spectrum2d(dcf_ctx *ctx, dcf_tree *tree, int attr1, const float *lvec1, int n1, int attr2,
                                   const float *lvec2, int n2, double *spectrum, int on_device);
 
+/* Direct-rule filter (dcf_filter with rule DCF_RULE_DIRECT) that allocates
+ * nothing.  No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory while filtering -- a host framework whose caching
+ * allocator already holds the device's free memory, or a real-time loop that must
+ * not wait on or fail in an allocation.  Its per-pixel scratch is a fixed 40 MiB
+ * device array inside the library (held by every GPU that loads it until exit), so
+ * the tree may have at most 8,388,608 pixels (DCF_ERR_INVALID beyond that).
+ * out_device must be device memory.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.  All
+ * calls share the one array: calls that overlap on the GPU (other streams or
+ * contexts) race and must not be issued concurrently. */
+dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, double lambda, int extract,
+                                     float *out_device);
+
 /* ---- lambda vectors ---- */
 /* Read a "#LambdaVector file..." file: out[0] = 0, out[i] = value_i / imscale.
  * *num_lambdas receives K+1; fails with DCF_ERR_INVALID if capacity < K+1. */
