@@ -485,13 +485,17 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
         ba.g = t->g;
         ba.kmax = t->stats + 1;
         ba.gval = t->gval;
+        void *nodes;
+        st = scratch(ctx, 9, (size_t)N * 8, &nodes);
+        if (st != DCF_OK) goto fail;
+        ba.node = (unsigned long long *)nodes;
         ba.parent = t->parent;
         ba.isroot = t->isroot;
         ba.num_nodes = t->num_nodes;
         ba.err = ctx->d_err;
         ba.sm_count = ctx->sm_count;
         launch_build(ba, ctx->stream);
-        st = check_launch(ctx, 5);
+        st = check_launch(ctx, 4);
         if (st != DCF_OK) goto fail;
     }
     if (tmp_in) {

@@ -5,13 +5,14 @@
 //   k_stats        min / max / NaN scan of the input (preprocessing.c:7-30).
 //   k_tile_build   one CTA builds the max-tree of one tile in shared memory: a 1-D
 //                  stack pass per row, then the rows are merged band by band with the
-//                  lock-free connect() on 16-bit shared-memory parents; the tile's
-//                  forest is written to HBM in canonical (level-root) form.
+//                  lock-free connect() on 64-bit shared-memory node words; the tile's
+//                  forest goes to the HBM node array in level-root form.
 //   k_seam_merge   every edge that crosses a tile boundary is merged with connect()
-//                  on the int32 parent array in HBM (32-bit CAS): the on-device
-//                  replacement of the MPI boundary-tree exchange and merge.
-//   k_canon_*      flatten to the reference's canonical form (flood.c:127-141,
-//                  get_levelroot :693-712): pixel -> level root, root -> parent's root.
+//                  on the HBM node array (64-bit CAS): the on-device replacement of
+//                  the MPI boundary-tree exchange and merge.
+//   k_canon        flatten to the reference's canonical form (flood.c:127-141,
+//                  get_levelroot :693-712) into the int32 parent array: pixel ->
+//                  level root, root -> parent's level root; root flags; node count.
 #include "dcf_kernels.cuh"
 
 namespace dcf {
@@ -50,39 +51,26 @@ __global__ void k_stats(const T *__restrict__ img, long long n, unsigned *kmin, 
 // ---------------------------------------------------------------------------
 // tile build
 // ---------------------------------------------------------------------------
-constexpr unsigned short SNONE = 0xFFFFu;
-
 struct SmemAcc {
-    const uint32_t *k;
-    unsigned short *p;
+    unsigned long long *w;
     unsigned *err;
-    __device__ uint32_t key(int i) const { return k[i]; }
+    __device__ uint64_t load(int i) const { return ((volatile unsigned long long *)w)[i]; }
+    __device__ void store(int i, uint64_t v) { ((volatile unsigned long long *)w)[i] = v; }
+    __device__ bool cas(int i, uint64_t expect, uint64_t v) { return atomicCAS(w + i, expect, v) == expect; }
     __device__ long long walk_bound() const { return TILE_PIX + 1; }
-    __device__ int par(int i) const
-    {
-        unsigned short v = ((volatile unsigned short *)p)[i];
-        return v == SNONE ? NONE : (int)v;
-    }
-    __device__ void set_par(int i, int v) { ((volatile unsigned short *)p)[i] = (unsigned short)v; }
-    __device__ bool cas_par(int i, int expect, int v)
-    {
-        unsigned short e = expect == NONE ? SNONE : (unsigned short)expect;
-        return atomicCAS(p + i, e, (unsigned short)v) == e;
-    }
     __device__ void error(unsigned bit) { raise_error(err, bit); }
 };
 
 template <typename T, bool MIN>
 __global__ void __launch_bounds__(TILE_THREADS)
 k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__restrict__ gval,
-             int *__restrict__ parent, unsigned *err)
+             unsigned long long *__restrict__ gnode, unsigned *err)
 {
     const float gmax = MIN ? key_to_level(*kmax) : 0.0f;
-    // tile extents: 2-D 64x64, 3-D 16x16x16 (4096 pixels, 16-bit local indices)
+    // tile extents: 2-D 64x64, 3-D 16x16x16 (4096 pixels, local indices < 2^16)
     const bool is3d = g.D > 1;
     const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
-    __shared__ uint32_t skey[TILE_PIX];
-    __shared__ unsigned short spar[TILE_PIX];
+    __shared__ unsigned long long snode[TILE_PIX];
     __shared__ unsigned short sstk[TILE_PIX];  // one TW-long stack per row
 
     const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, z0 = blockIdx.z * TD;
@@ -91,13 +79,14 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
 
     for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
         int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
-        spar[i] = SNONE;
+        uint32_t k = 0;
         if (lx < wl && ly < hl && lz < dl) {
             long long gp = (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
             float lv = level_of<T, MIN>(img[gp], gmax);
             gval[gp] = lv;
-            skey[i] = order_key(lv);
+            k = order_key(lv);
         }
+        snode[i] = wmake(k, NONE);
     }
     __syncthreads();
 
@@ -112,21 +101,21 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
         const int base = r * TW;
         for (int lx = 0; lx < wl; lx++) {
             int i = base + lx;
-            uint32_t ki = skey[i];
+            uint32_t ki = wkey(snode[i]);
             int last = NONE;
-            while (sp > 0 && skey[stk[sp - 1]] > ki) {
+            while (sp > 0 && wkey(snode[stk[sp - 1]]) > ki) {
                 int t = stk[--sp];
-                if (last != NONE) spar[last] = (unsigned short)t;
+                if (last != NONE) snode[last] = wmake(wkey(snode[last]), t);
                 last = t;
             }
-            if (last != NONE) spar[last] = (unsigned short)i;
+            if (last != NONE) snode[last] = wmake(wkey(snode[last]), i);
             stk[sp++] = (unsigned short)i;
         }
-        for (int j = sp - 1; j >= 1; j--) spar[stk[j]] = stk[j - 1];
+        for (int j = sp - 1; j >= 1; j--) snode[stk[j]] = wmake(wkey(snode[stk[j]]), stk[j - 1]);
     }
     __syncthreads();
 
-    SmemAcc acc{skey, spar, err};
+    SmemAcc acc{snode, err};
     const Offs offs = forward_offsets(g.conn);
     // merge row bands along y (each z slice), then slabs along z; at level k the
     // seams are the rows (slices) c with c % 2^(k+1) == 2^k
@@ -136,9 +125,7 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
             const int nseams = (ext + 2 * half - 1) / (2 * half);
             const int other = axis == 1 ? TD : TH;  // slices (axis y) or rows (axis z)
             // all edges across the seams of this level at once; correctness does not
-            // depend on the order (see connect), and for the deep chains of high
-            // dynamic-range tiles concurrent walkers finish sooner than any ordering
-            // by fewer threads
+            // depend on the order (see connect)
             const long long work = (long long)nseams * other * TW;
             for (long long w = tid; w < work; w += TILE_THREADS) {
                 int lx = (int)(w % TW);
@@ -165,31 +152,30 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
         }
     }
 
-    // canonical form inside the tile: pixel -> level root, root -> parent's level root
+    // level-root form inside the tile (read-only walks, then each pixel writes its
+    // own word): pixel -> level root, root -> parent's level root; to global indices
+    unsigned short *sroot = sstk;  // the row stacks are no longer needed
     for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
         int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
-        if (lx >= wl || ly >= hl || lz >= dl) continue;
-        int r = levelroot_ro(acc, i);
-        if (r != i) acc.set_par(i, r);
+        sroot[i] = (lx < wl && ly < hl && lz < dl) ? (unsigned short)levelroot_ro(acc, i) : (unsigned short)0xFFFFu;
     }
     __syncthreads();
     for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
         int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
         if (lx >= wl || ly >= hl || lz >= dl) continue;
-        int p = acc.par(i);
-        if (p != NONE && skey[p] < skey[i]) {  // level root: point at the parent's level root
-            int q = acc.par(p);
-            if (q != NONE && skey[q] == skey[p]) p = q;
+        const uint64_t w = snode[i];
+        int p = sroot[i];
+        if (p == i) {  // level root: its parent node's level root
+            const int q = wpar(w);
+            p = q == NONE ? NONE : (int)sroot[q];
         }
-        int out;
-        if (p == NONE) {
-            out = NONE;
-        } else {
+        int out = NONE;
+        if (p != NONE) {
             int px = p % TW, py = (p / TW) % TH, pz = p / (TW * TH);
             out = (int)((long long)(z0 + pz) * g.WH + (long long)(y0 + py) * g.W + (x0 + px));
         }
         long long gp = (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
-        parent[gp] = out;
+        gnode[gp] = wmake(wkey(w), out);
     }
 }
 
@@ -197,15 +183,13 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
 // seam merge in HBM
 // ---------------------------------------------------------------------------
 struct GlobalAcc {
-    const float *gv;
-    int *p;
+    unsigned long long *w;
     unsigned *err;
     long long n;
-    __device__ uint32_t key(int i) const { return order_key(gv[i]); }
+    __device__ uint64_t load(int i) const { return ((volatile unsigned long long *)w)[i]; }
+    __device__ void store(int i, uint64_t v) { ((volatile unsigned long long *)w)[i] = v; }
+    __device__ bool cas(int i, uint64_t expect, uint64_t v) { return atomicCAS(w + i, expect, v) == expect; }
     __device__ long long walk_bound() const { return n + 1; }
-    __device__ int par(int i) const { return ((volatile int *)p)[i]; }
-    __device__ void set_par(int i, int v) { ((volatile int *)p)[i] = v; }
-    __device__ bool cas_par(int i, int expect, int v) { return atomicCAS(p + i, expect, v) == expect; }
     __device__ void error(unsigned bit) { raise_error(err, bit); }
 };
 
@@ -214,19 +198,17 @@ struct GlobalAcc {
 // pixels one thread walks in order, merging every forward edge of each pixel that
 // leaves the tile.  Every cross-tile edge leaves its low endpoint's tile through
 // one of these faces, so all are merged (edges at tile corners possibly twice,
-// which is harmless); in-order processing keeps the merge walks short, as inside
-// the tile.
-constexpr int SEAM_SEG = 16;
+// which is harmless).
+constexpr int SEAM_SEG = 4;
 
 // largest face (2-D: a 64-pixel side; 3-D: a 16x16 face) in SEAM_SEG runs
 __host__ __device__ inline int seam_segments_per_face(bool is3d) { return is3d ? 256 / SEAM_SEG : 64 / SEAM_SEG; }
 
-__global__ void k_seam_merge(const float *__restrict__ gval, Geom g, int ntx, int nty, int ntz, int *parent,
-                             unsigned *err)
+__global__ void k_seam_merge(unsigned long long *gnode, Geom g, int ntx, int nty, int ntz, unsigned *err)
 {
     const bool is3d = g.D > 1;
     const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
-    GlobalAcc acc{gval, parent, err, g.N};
+    GlobalAcc acc{gnode, err, g.N};
     const Offs offs = forward_offsets(g.conn);
     bool neg_x = false, neg_y = false;
     for (int e = 0; e < offs.n; e++) {
@@ -267,35 +249,25 @@ __global__ void k_seam_merge(const float *__restrict__ gval, Geom g, int ntx, in
 }
 
 // ---------------------------------------------------------------------------
-// canonical form
+// canonical form: read-only walks on the node words, each pixel writes only its
+// own parent entry and root flag
 // ---------------------------------------------------------------------------
-__global__ void k_canon_pixels(const float *__restrict__ gval, Geom g, int *parent, unsigned *err)
+__global__ void k_canon(unsigned long long *gnode, Geom g, int *parent, unsigned char *isroot,
+                        unsigned long long *num_nodes, unsigned *err)
 {
-    GlobalAcc acc{gval, parent, err, g.N};
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
-         p += (long long)gridDim.x * blockDim.x) {
-        int r = levelroot_ro(acc, (int)p);
-        if (r != (int)p) acc.set_par((int)p, r);
-    }
-}
-
-__global__ void k_canon_roots(const float *__restrict__ gval, Geom g, int *parent, unsigned char *isroot,
-                              unsigned long long *num_nodes, unsigned *err)
-{
-    GlobalAcc acc{gval, parent, err, g.N};
+    GlobalAcc acc{gnode, err, g.N};
     unsigned cnt = 0;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
          p += (long long)gridDim.x * blockDim.x) {
-        int q = acc.par((int)p);
-        uint32_t kp = acc.key((int)p);
-        const bool root = q == NONE || acc.key(q) != kp;
-        isroot[p] = root ? 1 : 0;
-        if (root) {
+        const int r = levelroot_ro(acc, (int)p);
+        if (r != (int)p) {
+            parent[p] = r;
+            isroot[p] = 0;
+        } else {
+            const int q = wpar(acc.load((int)p));
+            parent[p] = q == NONE ? NONE : levelroot_ro(acc, q);
+            isroot[p] = 1;
             cnt++;
-            if (q != NONE) {
-                int r = acc.par(q);
-                if (r != NONE && acc.key(r) == acc.key(q)) acc.set_par((int)p, r);
-            }
         }
     }
     for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -313,20 +285,18 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
     const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
     dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
     prof_begin(P_TILE, s);
-    k_tile_build<T, MIN><<<grid, TILE_THREADS, 0, s>>>(img, a.g, a.kmax, a.gval, a.parent, a.err);
+    k_tile_build<T, MIN><<<grid, TILE_THREADS, 0, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err);
     prof_end(P_TILE, s);
-    int nb = grid_for(a.g.N, 256, a.sm_count);
     prof_begin(P_SEAM, s);
     {
         const int nseg_face = seam_segments_per_face(is3d);
         const long long work = (long long)grid.x * grid.y * grid.z * 5 * nseg_face;
-        k_seam_merge<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.gval, a.g, grid.x, grid.y, grid.z, a.parent,
-                                                                      a.err);
+        k_seam_merge<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err);
     }
     prof_end(P_SEAM, s);
+    int nb = grid_for(a.g.N, 256, a.sm_count);
     prof_begin(P_CANON, s);
-    k_canon_pixels<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.err);
-    k_canon_roots<<<nb, 256, 0, s>>>(a.gval, a.g, a.parent, a.isroot, a.num_nodes, a.err);
+    k_canon<<<nb, 256, 0, s>>>(a.node, a.g, a.parent, a.isroot, a.num_nodes, a.err);
     prof_end(P_CANON, s);
 }
 

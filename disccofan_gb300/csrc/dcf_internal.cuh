@@ -1,9 +1,11 @@
 // Internal device/host definitions shared by the CUDA translation units.
 //
 // Data layout in HBM (one tree):
-//   img      caller's pixels in their own type (u8/u16/u32/f32), x fastest;
-//            grey levels and sort keys are recomputed from it on the fly, so no
-//            per-pixel level or key array is stored.
+//   img      caller's pixels in their own type (u8/u16/u32/f32), x fastest; read
+//            once by the tile kernel.
+//   gval     float[N]: the grey levels (min-tree: inverted) every later pass uses.
+//   node     uint64[N] (build scratch): key and current parent of every pixel
+//            while trees are merged; see wmake/wkey/wpar.
 //   parent   int32[N]: canonical form after the build -- a pixel that is not a
 //            level root points to its node's level root (the lowest linear index
 //            of the node's flat zone, the reference's choice, flood.c:127-141); a
@@ -121,20 +123,49 @@ __host__ __device__ inline Offs forward_offsets(int conn)
 // component tree of all merged edges.  Path halving writes only shortcut
 // equal-key links, which no CAS can race with (a CAS expects a lower-key parent).
 // ---------------------------------------------------------------------------
-template <class A>
-__device__ __forceinline__ int levelroot(A &acc, int i)
+// Node words: one 64-bit word per pixel holds its immutable key (high half) and
+// its current parent (low half, 0xFFFFFFFF = none), so one dependent load yields
+// both the next node on a chain and the key needed to compare it, and a splice is a
+// single 64-bit CAS.
+__device__ __forceinline__ int wpar(uint64_t w)
 {
-    const uint32_t k = acc.key(i);
+    uint32_t p = (uint32_t)w;
+    return p == 0xFFFFFFFFu ? NONE : (int)p;
+}
+__device__ __forceinline__ uint32_t wkey(uint64_t w) { return (uint32_t)(w >> 32); }
+__device__ __forceinline__ uint64_t wmake(uint32_t key, int par)
+{
+    return ((uint64_t)key << 32) | (uint32_t)(par == NONE ? 0xFFFFFFFFu : (uint32_t)par);
+}
+
+// Level root of i (follows equal-key links); on return i is the root and w its word.
+// Path halving shortcuts equal-key links while walking.
+template <class A>
+__device__ __forceinline__ void levelroot(A &acc, int &i, uint64_t &w)
+{
+    w = acc.load(i);
+    const uint32_t k = wkey(w);
     const long long bound = acc.walk_bound();
     for (long long it = 0; it < bound; it++) {
-        int p = acc.par(i);
-        if (p == NONE || acc.key(p) != k) return i;
-        int pp = acc.par(p);
-        if (pp != NONE && acc.key(pp) == k) acc.set_par(i, pp);
+        const int p = wpar(w);
+        if (p == NONE) return;
+        const uint64_t wp = acc.load(p);
+        if (wkey(wp) != k) return;
+        const int pp = wpar(wp);
+        if (pp != NONE) {
+            const uint64_t wpp = acc.load(pp);
+            if (wkey(wpp) == k) {
+                acc.store(i, wmake(k, pp));
+                i = pp;
+                w = wpp;
+                continue;
+            }
+        }
         i = p;
+        w = wp;
+        return;
     }
     acc.error(DEVERR_WALK_BOUND);
-    return i;
 }
 
 // Read-only level-root walk for the final canonicalisation passes: there every
@@ -143,12 +174,16 @@ __device__ __forceinline__ int levelroot(A &acc, int i)
 template <class A>
 __device__ __forceinline__ int levelroot_ro(A &acc, int i)
 {
-    const uint32_t k = acc.key(i);
+    uint64_t w = acc.load(i);
+    const uint32_t k = wkey(w);
     const long long bound = acc.walk_bound();
     for (long long it = 0; it < bound; it++) {
-        int p = acc.par(i);
-        if (p == NONE || acc.key(p) != k) return i;
+        const int p = wpar(w);
+        if (p == NONE) return i;
+        const uint64_t wp = acc.load(p);
+        if (wkey(wp) != k) return i;
         i = p;
+        w = wp;
     }
     acc.error(DEVERR_WALK_BOUND);
     return i;
@@ -157,29 +192,40 @@ __device__ __forceinline__ int levelroot_ro(A &acc, int i)
 template <class A>
 __device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
 {
+    uint64_t wa, wb;
+    levelroot(acc, a, wa);
+    levelroot(acc, b, wb);
     for (long long it = 0; it < bound; it++) {
-        a = levelroot(acc, a);
-        b = levelroot(acc, b);
         if (a == b) return;
-        uint32_t ka = acc.key(a), kb = acc.key(b);
+        uint32_t ka = wkey(wa), kb = wkey(wb);
         if (ka < kb || (ka == kb && a < b)) {
             int t = a; a = b; b = t;
+            uint64_t tw = wa; wa = wb; wb = tw;
             uint32_t tk = ka; ka = kb; kb = tk;
         }
         // a sits above b: ka > kb, or equal keys with a > b (a's node joins b's)
-        int pa = acc.par(a);
+        const int pa = wpar(wa);
+        int lpa = pa;
+        uint64_t wl = 0;
         if (pa != NONE) {
-            int lpa = levelroot(acc, pa);
+            levelroot(acc, lpa, wl);
             if (lpa == b) return;
-            if (acc.key(lpa) >= kb) {  // b belongs below a's parent node: descend
+            if (wkey(wl) >= kb) {  // b belongs below a's parent node: descend
                 a = lpa;
+                wa = wl;
                 continue;
             }
         }
-        if (acc.cas_par(a, pa, b)) {
+        if (acc.cas(a, wa, wmake(ka, b))) {
             if (pa == NONE) return;
+            // merge the displaced tail (a's old parent node) into b's chain
             a = b;
-            b = pa;
+            wa = wb;
+            b = lpa;
+            wb = wl;
+        } else {
+            levelroot(acc, a, wa);
+            levelroot(acc, b, wb);
         }
     }
     acc.error(DEVERR_MERGE_BOUND);

@@ -35,6 +35,7 @@ struct BuildArgs {
     Geom g;
     const unsigned *kmax;            // order key of the maximum level (min-tree inversion)
     float *gval;
+    unsigned long long *node;        // N node words (build scratch)
     int *parent;
     unsigned char *isroot;
     unsigned long long *num_nodes;
