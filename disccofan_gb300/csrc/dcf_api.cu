@@ -37,6 +37,9 @@ struct dcf_ctx {
     char last_error[512] = {0};
     uint64_t launches = 0;
     int up_steps = 2048;              // bottom-up fold steps per walker before pointer jumping
+    int tile2d[2] = {64, 64};         // build tile of 2-D images (width, height)
+    int tile3d[3] = {16, 16, 16};     // build tile of 3-D images
+    int level_sync = 1;               // barrier between band-merge levels inside a tile
     std::mutex trees_mu;
     std::set<dcf_tree *> trees;       // live trees; orphaned (stream cleared) when the context goes
     DevBuf scratch[12];               // reusable work buffers (filter, spectra, attributes)
@@ -227,6 +230,14 @@ dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out)
         ctx->own_stream = true;
     }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (const char *e = getenv("DCF_TILE2D")) {  // e.g. "32x32"
+        int a = 0, b = 0;
+        if (sscanf(e, "%dx%d", &a, &b) == 2 && a > 0 && b > 0 && a * b <= TILE_MAX_PIX) {
+            ctx->tile2d[0] = a;
+            ctx->tile2d[1] = b;
+        }
+    }
+    if (const char *e = getenv("DCF_LEVEL_SYNC")) ctx->level_sync = atoi(e) != 0;
     if (const char *e = getenv("DCF_UP_STEPS")) {
         int v = atoi(e);
         if (v >= 0 && v < (1 << 20)) ctx->up_steps = v;
@@ -444,6 +455,16 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
     t->g.WH = (long long)W * H;
     t->g.N = (long long)N;
     t->g.conn = conn;
+    t->g.level_sync = ctx->level_sync;
+    if (D > 1) {
+        t->g.tw = ctx->tile3d[0];
+        t->g.th = ctx->tile3d[1];
+        t->g.td = ctx->tile3d[2];
+    } else {
+        t->g.tw = ctx->tile2d[0];
+        t->g.th = ctx->tile2d[1];
+        t->g.td = 1;
+    }
     t->dtype = img->dtype;
     t->tree_min = img->tree_type == DCF_MIN_TREE;
     for (int i = 0; i < 3; i++) t->pixdim[i] = img->pixdim[i];

@@ -41,13 +41,19 @@ __global__ void k_attr_pixels(const float *__restrict__ gval, Geom g, const int 
         if (G == 0 || !valid) continue;
         const unsigned x = (unsigned)(p % g.W), y = (unsigned)((p / g.W) % g.H), z = (unsigned)(p / g.WH);
         if (G == 1) {
-            atomicMin(a.bmin[0] + node, x);
-            atomicMin(a.bmin[1] + node, y);
-            atomicMax(a.bmax[0] + node, x + 1);
-            atomicMax(a.bmax[1] + node, y + 1);
-            if (a.has_z) {
-                atomicMin(a.bmin[2] + node, z);
-                atomicMax(a.bmax[2] + node, z + 1);
+            // lanes of one node reduce first; their leader issues the atomics
+            const unsigned mnx = __reduce_min_sync(grp, x), mny = __reduce_min_sync(grp, y);
+            const unsigned mxx = __reduce_max_sync(grp, x + 1), mxy = __reduce_max_sync(grp, y + 1);
+            const unsigned mnz = __reduce_min_sync(grp, z), mxz = __reduce_max_sync(grp, z + 1);
+            if (lane == __ffs(grp) - 1) {
+                atomicMin(a.bmin[0] + node, mnx);
+                atomicMin(a.bmin[1] + node, mny);
+                atomicMax(a.bmax[0] + node, mxx);
+                atomicMax(a.bmax[1] + node, mxy);
+                if (a.has_z) {
+                    atomicMin(a.bmin[2] + node, mnz);
+                    atomicMax(a.bmax[2] + node, mxz);
+                }
             }
             continue;
         }

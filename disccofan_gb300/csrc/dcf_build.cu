@@ -54,26 +54,30 @@ __global__ void k_stats(const T *__restrict__ img, long long n, unsigned *kmin, 
 struct SmemAcc {
     unsigned long long *w;
     unsigned *err;
+    int npix;
     __device__ uint64_t load(int i) const { return ((volatile unsigned long long *)w)[i]; }
     __device__ void store(int i, uint64_t v) { ((volatile unsigned long long *)w)[i] = v; }
     __device__ bool cas(int i, uint64_t expect, uint64_t v) { return atomicCAS(w + i, expect, v) == expect; }
-    __device__ long long walk_bound() const { return TILE_PIX + 1; }
+    __device__ long long walk_bound() const { return npix + 1; }
     __device__ void error(unsigned bit) { raise_error(err, bit); }
 };
 
+// Max-tree of one tile by the whole CTA.  The tile starts at (x0, y0, z0) of an
+// image of geometry g whose pixel (x, y, z) has global index off + z*WH + y*W + x
+// (off > 0 for one cutout of a batch).  smem holds tw*th*td node words followed by
+// the row stacks.  Writes gval and the tile forest (level-root form, global
+// indices) into gnode.
 template <typename T, bool MIN>
-__global__ void __launch_bounds__(TILE_THREADS)
-k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__restrict__ gval,
-             unsigned long long *__restrict__ gnode, unsigned *err)
+__device__ __forceinline__ void build_tile(const T *__restrict__ img, long long off, const Geom &g, int x0, int y0,
+                                           int z0, float gmax, float *__restrict__ gval,
+                                           unsigned long long *__restrict__ gnode, unsigned *err,
+                                           unsigned long long *smem_tile)
 {
-    const float gmax = MIN ? key_to_level(*kmax) : 0.0f;
-    // tile extents: 2-D 64x64, 3-D 16x16x16 (4096 pixels, local indices < 2^16)
+    // tile extents from the geometry (at most 4096 pixels: local indices < 2^16)
     const bool is3d = g.D > 1;
-    const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
-    __shared__ unsigned long long snode[TILE_PIX];
-    __shared__ unsigned short sstk[TILE_PIX];  // one TW-long stack per row
-
-    const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, z0 = blockIdx.z * TD;
+    const int TW = g.tw, TH = g.th, TD = g.td, TILE_PIX = TW * TH * TD;
+    unsigned long long *snode = smem_tile;                               // TILE_PIX words
+    unsigned short *sstk = (unsigned short *)(smem_tile + TILE_PIX);     // one TW-long stack per row
     const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
     const int tid = threadIdx.x;
 
@@ -81,7 +85,7 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
         int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
         uint32_t k = 0;
         if (lx < wl && ly < hl && lz < dl) {
-            long long gp = (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
+            long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
             float lv = level_of<T, MIN>(img[gp], gmax);
             gval[gp] = lv;
             k = order_key(lv);
@@ -115,7 +119,7 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
     }
     __syncthreads();
 
-    SmemAcc acc{snode, err};
+    SmemAcc acc{snode, err, TILE_PIX};
     const Offs offs = forward_offsets(g.conn);
     // merge row bands along y (each z slice), then slabs along z; at level k the
     // seams are the rows (slices) c with c % 2^(k+1) == 2^k
@@ -148,9 +152,12 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
                     connect(acc, p, qx + qy * TW + qz * TW * TH, MERGE_BOUND_SMEM);
                 }
             }
-            __syncthreads();
+            // levels are ordered for shorter merge walks, not for correctness:
+            // without the barrier warps run ahead into the next level
+            if (g.level_sync) __syncthreads();
         }
     }
+    __syncthreads();
 
     // level-root form inside the tile (read-only walks, then each pixel writes its
     // own word): pixel -> level root, root -> parent's level root; to global indices
@@ -172,11 +179,22 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
         int out = NONE;
         if (p != NONE) {
             int px = p % TW, py = (p / TW) % TH, pz = p / (TW * TH);
-            out = (int)((long long)(z0 + pz) * g.WH + (long long)(y0 + py) * g.W + (x0 + px));
+            out = (int)(off + (long long)(z0 + pz) * g.WH + (long long)(y0 + py) * g.W + (x0 + px));
         }
-        long long gp = (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
+        long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
         gnode[gp] = wmake(wkey(w), out);
     }
+}
+
+template <typename T, bool MIN>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__restrict__ gval,
+             unsigned long long *__restrict__ gnode, unsigned *err)
+{
+    extern __shared__ unsigned long long smem_tile[];
+    const float gmax = MIN ? key_to_level(*kmax) : 0.0f;
+    build_tile<T, MIN>(img, 0, g, blockIdx.x * g.tw, blockIdx.y * g.th, blockIdx.z * g.td, gmax, gval, gnode, err,
+                       smem_tile);
 }
 
 // ---------------------------------------------------------------------------
@@ -201,13 +219,19 @@ struct GlobalAcc {
 // which is harmless).
 constexpr int SEAM_SEG = 4;
 
-// largest face (2-D: a 64-pixel side; 3-D: a 16x16 face) in SEAM_SEG runs
-__host__ __device__ inline int seam_segments_per_face(bool is3d) { return is3d ? 256 / SEAM_SEG : 64 / SEAM_SEG; }
+// largest tile face in SEAM_SEG runs
+__host__ __device__ inline int seam_segments_per_face(const Geom &g)
+{
+    int f = g.th * g.td;
+    f = f > g.tw * g.td ? f : g.tw * g.td;
+    if (g.D > 1) f = f > g.tw * g.th ? f : g.tw * g.th;
+    return (f + SEAM_SEG - 1) / SEAM_SEG;
+}
 
 __global__ void k_seam_merge(unsigned long long *gnode, Geom g, int ntx, int nty, int ntz, unsigned *err)
 {
     const bool is3d = g.D > 1;
-    const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
+    const int TW = g.tw, TH = g.th, TD = g.td;
     GlobalAcc acc{gnode, err, g.N};
     const Offs offs = forward_offsets(g.conn);
     bool neg_x = false, neg_y = false;
@@ -217,7 +241,7 @@ __global__ void k_seam_merge(unsigned long long *gnode, Geom g, int ntx, int nty
     }
     // face f: 0 +x, 1 -x, 2 +y, 3 -y, 4 +z; pixels per face and segments per face
     const int fpix[5] = {TH * TD, TH * TD, TW * TD, TW * TD, TW * TH};
-    const int nseg_face = seam_segments_per_face(is3d);
+    const int nseg_face = seam_segments_per_face(g);
     const long long ntiles = (long long)ntx * nty * ntz;
     const long long work = ntiles * 5 * nseg_face;
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
@@ -281,15 +305,15 @@ template <typename T, bool MIN>
 static void build_t(const BuildArgs &a, cudaStream_t s)
 {
     const T *img = (const T *)a.img;
-    const bool is3d = a.g.D > 1;
-    const int TW = is3d ? 16 : 64, TH = is3d ? 16 : 64, TD = is3d ? 16 : 1;
+    const int TW = a.g.tw, TH = a.g.th, TD = a.g.td;
     dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
+    const size_t smem = (size_t)TW * TH * TD * (8 + 2);
     prof_begin(P_TILE, s);
-    k_tile_build<T, MIN><<<grid, TILE_THREADS, 0, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err);
+    k_tile_build<T, MIN><<<grid, TILE_THREADS, smem, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err);
     prof_end(P_TILE, s);
     prof_begin(P_SEAM, s);
     {
-        const int nseg_face = seam_segments_per_face(is3d);
+        const int nseg_face = seam_segments_per_face(a.g);
         const long long work = (long long)grid.x * grid.y * grid.z * 5 * nseg_face;
         k_seam_merge<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err);
     }

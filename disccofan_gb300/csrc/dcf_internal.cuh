@@ -35,6 +35,8 @@ struct Geom {
     long long WH;
     long long N;
     int conn;
+    int tw, th, td;  // build tile extents (tw*th*td <= 4096)
+    int level_sync;  // barrier between the band-merge levels of a tile
 };
 
 // Grey level as the reference holds it (types.h:53 `value` = float): the pixel

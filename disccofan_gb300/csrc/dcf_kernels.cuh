@@ -15,7 +15,7 @@ void prof_begin(int id, cudaStream_t s);
 void prof_end(int id, cudaStream_t s);
 
 constexpr int TILE_THREADS = 256;
-constexpr int TILE_PIX = 4096;                 // 64x64 (2-D) or 16x16x16 (3-D)
+constexpr int TILE_MAX_PIX = 4096;             // largest build tile (16-bit local indices)
 constexpr long long MERGE_BOUND_SMEM = 1LL << 22;
 constexpr long long MERGE_BOUND_GLOBAL = 1LL << 28;
 
