@@ -48,6 +48,28 @@ class _Image(C.Structure):
                 ("connectivity", C.c_int), ("tree_type", C.c_int), ("pixdim", C.c_float * 3)]
 
 
+class OpSet(C.Structure):
+    """dcf_op_set: the operations of a batch run / an adjoint."""
+    _fields_ = [("filter_attr", C.c_int), ("lam", C.c_double), ("spec_attr1", C.c_int), ("lvec1", C.c_void_p),
+                ("n1", C.c_int), ("spec_attr2", C.c_int), ("lvec2", C.c_void_p), ("n2", C.c_int),
+                ("use_graph", C.c_int)]
+
+
+def make_ops(filter_attr=-1, lam=0.0, spectrum=None, use_graph=False):
+    """OpSet plus the lambda arrays it points to (keep both alive).  spectrum =
+    (attr1, lvec1, attr2, lvec2) with lvecs including the leading 0."""
+    keep = []
+    ops = OpSet(filter_attr, float(lam), -1, None, 0, 0, None, 0, int(use_graph))
+    if spectrum is not None:
+        a1, l1, a2, l2 = spectrum
+        l1 = np.ascontiguousarray(l1, np.float32)
+        l2 = np.ascontiguousarray(l2, np.float32)
+        keep += [l1, l2]
+        ops.spec_attr1, ops.lvec1, ops.n1 = a1, l1.ctypes.data, l1.size
+        ops.spec_attr2, ops.lvec2, ops.n2 = a2, l2.ctypes.data, l2.size
+    return ops, keep
+
+
 _lib = None
 _exiting = False
 
@@ -89,6 +111,16 @@ def library() -> C.CDLL:
         "dcf_pattern_spectrum": [vp, vp, i, vp, i, vp, i],
         "dcf_pattern_spectrum2d": [vp, vp, i, vp, i, i, vp, i, vp, i],
         "dcf_lvec_read": [C.c_char_p, d, vp, i, C.POINTER(i)],
+        "dcf_batch_create": [vp, i, vp, vp, i, i, i, vp, C.POINTER(vp)],
+        "dcf_batch_destroy": [vp],
+        "dcf_batch_info": [vp, C.POINTER(u64), C.POINTER(u64), vp, C.POINTER(u64)],
+        "dcf_batch_set_schedule": [vp, vp, i, i, i, i],
+        "dcf_batch_autotune": [vp, vp, vp, i, i, C.POINTER(d)],
+        "dcf_batch_run": [vp, vp, vp, i, C.POINTER(OpSet), vp, vp, i],
+        "dcf_batch_parent": [vp, vp, vp, i],
+        "dcf_batch_node_attribute": [vp, vp, i, vp, i],
+        "dcf_batch_adjoint": [vp, vp, vp, vp, vp, i],
+        "dcf_tree_adjoint": [vp, vp, C.POINTER(OpSet), vp, vp, vp, i],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -190,6 +222,11 @@ class Context:
               pixdim=(1.0, 1.0, 1.0)) -> "Tree":
         """build_tree_with_attributes: tree of a 2-D (H, W) or 3-D (D, H, W) image."""
         return Tree(self, image, connectivity, tree_type, attribute, pixdim)
+
+    def batch(self, shapes, dtype=np.float32, connectivity: int = 8, attribute: int = 0,
+              pixdim=(1.0, 1.0, 1.0)) -> "Batch":
+        """A batch of 2-D cutouts; shapes = [(height, width), ...]."""
+        return Batch(self, shapes, dtype, connectivity, attribute, pixdim)
 
 
 class Tree:
@@ -337,3 +374,150 @@ class Tree:
         self.ctx.check(self.ctx.lib.dcf_pattern_spectrum2d(self.ctx.h, self.h, attr1, l1.ctypes.data, l1.size, attr2,
                                                            l2.ctypes.data, l2.size, p, dev), "pattern_spectrum2d")
         return spec
+
+    # -- adjoint -------------------------------------------------------------
+    def adjoint(self, grad_filtered=None, filter_attr: int = -1, lam: float = 0.0, grad_spectrum=None,
+                spectrum=None, out=None):
+        """d loss / d pixels of loss = sum(grad_filtered * filter(filter_attr, lam, "direct"))
+        + sum(grad_spectrum * pattern_spectrum2d(*spectrum)), this tree held fixed
+        (float32 max-trees).  grad_spectrum has the [n2, n1] layout of pattern_spectrum2d."""
+        ops, keep = make_ops(filter_attr, lam, spectrum)
+        dev = int(out is not None and _is_torch_cuda(out))
+
+        def ptr(x, dt):
+            if x is None:
+                return None, None
+            if dev:
+                return x, x.data_ptr()
+            a = np.ascontiguousarray(x, dt)
+            return a, a.ctypes.data
+        v, vp = ptr(grad_filtered, np.float32)
+        w, wp = ptr(grad_spectrum, np.float64)
+        a, p, _ = self._out(np.float32, out)
+        self.ctx.check(self.ctx.lib.dcf_tree_adjoint(self.ctx.h, self.h, C.byref(ops), vp, wp, p, dev), "adjoint")
+        return self._shape(a)
+
+
+class Batch:
+    """Many 2-D cutouts built, filtered and binned together (dcf_batch)."""
+
+    def __init__(self, ctx: Context, shapes, dtype, connectivity, attribute, pixdim):
+        self.ctx = ctx
+        self.shapes = [(int(h), int(w)) for h, w in shapes]
+        self.dtype = np.dtype(dtype)
+        hs = np.array([h for h, _ in self.shapes], np.uint32)
+        ws = np.array([w for _, w in self.shapes], np.uint32)
+        sizes = hs.astype(np.int64) * ws
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+        self.n = int(sizes.sum())
+        self.count = len(self.shapes)
+        pd = (C.c_float * 3)(*pixdim)
+        hnd = C.c_void_p()
+        ctx.check(ctx.lib.dcf_batch_create(ctx.h, self.count, ws.ctypes.data, hs.ctypes.data, DTYPES[self.dtype],
+                                           connectivity, attribute, pd, C.byref(hnd)), "dcf_batch_create")
+        self.h = hnd
+        self.attribute = attribute
+        self._keep = None
+
+    def close(self):
+        if getattr(self, "h", None) and not _exiting:
+            self.ctx.lib.dcf_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def concat(self, cutouts) -> np.ndarray:
+        """Concatenate host cutouts (each (H, W)) in the batch's pixel order."""
+        return np.concatenate([np.ascontiguousarray(c, self.dtype).ravel() for c in cutouts])
+
+    def split(self, flat):
+        """Per-cutout (H, W) views of a concatenated per-pixel array."""
+        return [flat[o:o + h * w].reshape(h, w) for o, (h, w) in zip(self.offsets, self.shapes)]
+
+    def _pixels(self, pixels):
+        if _is_torch_cuda(pixels):
+            return pixels.data_ptr(), 1
+        a = np.ascontiguousarray(pixels, self.dtype).ravel()
+        if a.size != self.n:
+            raise ValueError(f"expected {self.n} pixels, got {a.size}")
+        self._keep = a
+        return a.ctypes.data, 0
+
+    def info(self):
+        n, m, g = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        sch = (C.c_int * 4)()
+        self.ctx.check(self.ctx.lib.dcf_batch_info(self.h, C.byref(n), C.byref(m), sch, C.byref(g)), "batch_info")
+        return {"pixels": n.value, "nodes": m.value, "tile": (sch[0], sch[1]), "ctas_per_sm": sch[2],
+                "chunk": sch[3], "graph_kernels": g.value}
+
+    def set_schedule(self, tile=(64, 64), ctas_per_sm=0, chunk=1):
+        self.ctx.check(self.ctx.lib.dcf_batch_set_schedule(self.ctx.h, self.h, tile[0], tile[1], ctas_per_sm, chunk),
+                       "set_schedule")
+
+    def autotune(self, pixels, repeats: int = 3) -> float:
+        p, dev = self._pixels(pixels)
+        ms = C.c_double()
+        self.ctx.check(self.ctx.lib.dcf_batch_autotune(self.ctx.h, self.h, p, dev, repeats, C.byref(ms)), "autotune")
+        return ms.value
+
+    def run(self, pixels, filter_attr: int = -1, lam: float = 0.0, spectrum=None, use_graph: bool = True,
+            filtered=None, spectra=None, want_filtered: bool = True, want_spectra: bool = True):
+        """Build all trees, then filter and/or bin.  pixels: host array (concatenated or
+        a list of cutouts) or a CUDA tensor of N elements.  Outputs go to `filtered` /
+        `spectra` when given (CUDA tensors: device outputs), else new host arrays.
+        Returns (filtered[N] or None, spectra[count, n2, n1] or None)."""
+        if isinstance(pixels, (list, tuple)):
+            pixels = self.concat(pixels)
+        p, pdev = self._pixels(pixels)
+        ops, keep = make_ops(filter_attr, lam, spectrum, use_graph)
+        odev = int((filtered is not None and _is_torch_cuda(filtered)) or
+                   (spectra is not None and _is_torch_cuda(spectra)))
+        f = s = None
+        if filter_attr >= 0 and want_filtered:
+            f = filtered if filtered is not None else np.empty(self.n, np.float32)
+        if spectrum is not None and want_spectra:
+            s = spectra if spectra is not None else np.empty((self.count, ops.n2, ops.n1), np.float64)
+        fp = (f.data_ptr() if odev else f.ctypes.data) if f is not None else None
+        sp = (s.data_ptr() if odev else s.ctypes.data) if s is not None else None
+        self.ctx.check(self.ctx.lib.dcf_batch_run(self.ctx.h, self.h, p, pdev, C.byref(ops), fp, sp, odev),
+                       "batch_run")
+        self._ops_keep = keep
+        return f, s
+
+    def parent(self, out=None):
+        """Canonical parents, as indices inside each cutout (concatenated)."""
+        a = out if out is not None else np.empty(self.n, np.int64)
+        dev = int(_is_torch_cuda(a))
+        self.ctx.check(self.ctx.lib.dcf_batch_parent(self.ctx.h, self.h, a.data_ptr() if dev else a.ctypes.data, dev),
+                       "batch_parent")
+        return a
+
+    def node_attribute(self, attribute: int, out=None):
+        a = out if out is not None else np.empty(self.n, np.float64)
+        dev = int(_is_torch_cuda(a))
+        self.ctx.check(self.ctx.lib.dcf_batch_node_attribute(self.ctx.h, self.h, attribute,
+                                                             a.data_ptr() if dev else a.ctypes.data, dev),
+                       "batch_node_attribute")
+        return a
+
+    def adjoint(self, grad_filtered=None, grad_spectra=None, out=None):
+        """d loss / d pixels for the last run's operations (trees held fixed)."""
+        dev = int(out is not None and _is_torch_cuda(out))
+        if dev:
+            vp = grad_filtered.data_ptr() if grad_filtered is not None else None
+            wp = grad_spectra.data_ptr() if grad_spectra is not None else None
+            g = out
+            gp = out.data_ptr()
+        else:
+            v = None if grad_filtered is None else np.ascontiguousarray(grad_filtered, np.float32).ravel()
+            w = None if grad_spectra is None else np.ascontiguousarray(grad_spectra, np.float64).ravel()
+            vp = v.ctypes.data if v is not None else None
+            wp = w.ctypes.data if w is not None else None
+            g = np.empty(self.n, np.float32)
+            gp = g.ctypes.data
+        self.ctx.check(self.ctx.lib.dcf_batch_adjoint(self.ctx.h, self.h, vp, wp, gp, dev), "batch_adjoint")
+        return g

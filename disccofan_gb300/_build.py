@@ -13,7 +13,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdcf_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_UNITS = ["dcf_build.cu", "dcf_attr.cu", "dcf_ops.cu", "dcf_api.cu"]
+CU_UNITS = ["dcf_build.cu", "dcf_attr.cu", "dcf_ops.cu", "dcf_batch.cu", "dcf_api.cu"]
 C_UNITS = ["dcf_host.c"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVFLAGS = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",

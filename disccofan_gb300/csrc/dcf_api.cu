@@ -2,6 +2,7 @@
 // host, enqueues kernels on the context's stream and only synchronises when it
 // must hand data back to host memory; device-side failures (loop bounds) are
 // collected in a device error word and reported by the next synchronising call.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -10,6 +11,7 @@
 #include <new>
 #include <set>
 #include <string>
+#include <vector>
 
 #include "../../include/dcf.h"
 #include "dcf_kernels.cuh"
@@ -360,25 +362,22 @@ static TreeView view_of(const dcf_tree *t)
     return v;
 }
 
-// allocate and accumulate the records of attr_idx's group
-static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
+// Record arrays of an attribute group over N pixels, carved from one allocation:
+// 64-bit arrays first (alignment), then 32-bit ones.
+static size_t attr_bytes(int group, size_t N)
 {
-    const int group = ATTR_GROUP[attr_idx];
-    if (t->attr_mem && t->attr.group == group) {
-        t->attr_idx = attr_idx;
-        return DCF_OK;
-    }
-    free_attr(t);
-    const size_t N = (size_t)t->g.N;
     const size_t n32 = 1 + 1 + (group == 1 ? 6 : 0);                                  // area, pending, bbox
     const size_t n64 = (group == 2 ? 3 : 0) + (group == 3 ? 5 : 0) + (group == 4 ? 14 : 0);
-    const size_t bytes = (n32 * 4 + n64 * 8) * N + 256;
-    CU(cudaMallocAsync(&t->attr_mem, bytes, ctx->stream));
-    char *m = (char *)t->attr_mem;
-    AttrBufs &a = t->attr;
+    return (n32 * 4 + n64 * 8) * N + 256;
+}
+
+static void attr_carve(AttrBufs &a, int group, bool exact_g, bool has_z, size_t N, void *mem)
+{
+    char *m = (char *)mem;
+    a = AttrBufs();
     a.group = group;
-    a.exact_g = t->dtype == U8 || t->dtype == U16;
-    // 64-bit arrays first (alignment), then 32-bit
+    a.exact_g = exact_g;
+    a.has_z = has_z;
     auto take64 = [&]() { void *p = m; m += 8 * N; return p; };
     if (group == 2) for (int d = 0; d < 3; d++) a.s1[d] = (unsigned long long *)take64();
     if (group == 4) {
@@ -393,13 +392,33 @@ static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
         for (int d = 0; d < 3; d++) a.bmin[d] = (uint32_t *)take32();
         for (int d = 0; d < 3; d++) a.bmax[d] = (uint32_t *)take32();
     }
-    // zero everything, then bbox minima to all-ones
-    CU(cudaMemsetAsync(t->attr_mem, 0, (size_t)(m - (char *)t->attr_mem), ctx->stream));
-    a.has_z = t->g.D > 1;
-    if (group == 1) {
-        CU(cudaMemsetAsync(a.bmin[0], 0xFF, (a.has_z ? 3 : 2) * 4 * N, ctx->stream));
-        if (!a.has_z) launch_fill_u32((long long)N, a.bmax[2], 1u, ctx->sm_count, ctx->stream);
+}
+
+// zero every record, bounding-box minima to all-ones, 2-D z extent to [0, 1)
+static cudaError_t attr_zero(const AttrBufs &a, size_t N, void *mem, int sm, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(mem, 0, attr_bytes(a.group, N) - 256, s);
+    if (e == cudaSuccess && a.group == 1) {
+        e = cudaMemsetAsync(a.bmin[0], 0xFF, (a.has_z ? 3 : 2) * 4 * N, s);
+        if (!a.has_z) launch_fill_u32((long long)N, a.bmax[2], 1u, sm, s);
     }
+    return e;
+}
+
+// allocate and accumulate the records of attr_idx's group
+static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
+{
+    const int group = ATTR_GROUP[attr_idx];
+    if (t->attr_mem && t->attr.group == group) {
+        t->attr_idx = attr_idx;
+        return DCF_OK;
+    }
+    free_attr(t);
+    const size_t N = (size_t)t->g.N;
+    CU(cudaMallocAsync(&t->attr_mem, attr_bytes(group, N), ctx->stream));
+    AttrBufs &a = t->attr;
+    attr_carve(a, group, t->dtype == U8 || t->dtype == U16, t->g.D > 1, N, t->attr_mem);
+    CU(attr_zero(a, N, t->attr_mem, ctx->sm_count, ctx->stream));
     unsigned *count = ctx->d_err + 2;
     launch_attributes(view_of(t), a, count, ctx->up_steps, ctx->d_err, ctx->sm_count, ctx->stream);
     dcf_status st = check_launch(ctx, 4);
@@ -884,3 +903,783 @@ extern "C" dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *t, int a
                   ctx->sm_count, ctx->stream);
     return check_launch(ctx, 3);
 }
+
+// ---------------------------------------------------------------------------
+// Batches of 2-D cutouts and the adjoint (no reference counterpart).
+//
+// A batch owns every device buffer its runs need, allocated once at creation (or
+// on the first run that needs it), so a run issues no allocation and can be
+// recorded as one CUDA graph: statistics, persistent tile build, seam merge,
+// canonical form, attribute pass, filter and spectra.  The only step that would
+// need the host in the middle is the attribute pass's pointer-jumping phase,
+// whose scratch is sized by the number of nodes left after the bounded
+// bottom-up fold; a graph run uses a fixed capacity learned on the first
+// (ungraphed) run, and a run whose count exceeds it is detected after the graph,
+// redone ungraphed and the capacity doubled.
+// ---------------------------------------------------------------------------
+struct BatchKey {
+    const void *pixels = nullptr;
+    float *filtered = nullptr;
+    double *spectra = nullptr;
+    int filter_attr = -1, a1 = -1, a2 = -1, n1 = 0, n2 = 0;
+    double lambda = 0.0;
+    int tw = 0, th = 0, ctas = 0, chunk = 0;
+    unsigned cap = 0;
+    void *rest_mem = nullptr;
+    bool operator==(const BatchKey &o) const
+    {
+        return pixels == o.pixels && filtered == o.filtered && spectra == o.spectra && filter_attr == o.filter_attr &&
+               a1 == o.a1 && a2 == o.a2 && n1 == o.n1 && n2 == o.n2 && lambda == o.lambda && tw == o.tw &&
+               th == o.th && ctas == o.ctas && chunk == o.chunk && cap == o.cap && rest_mem == o.rest_mem;
+    }
+};
+
+struct dcf_batch {
+    dcf_ctx *ctx = nullptr;
+    int count = 0, dtype = F32, conn = 8, group = 0, attr_idx = 0;
+    float pixdim[3] = {1, 1, 1};
+    long long N = 0;
+    std::vector<BatchImg> imgs;
+    BatchImg *d_imgs = nullptr;
+    long long *d_offs = nullptr;
+    // schedule: tile shape, CTAs per SM of the persistent kernel, tiles per queue grab
+    int tw = 64, th = 64, ctas = 1, chunk = 1;
+    int ntiles = 0;
+    size_t tiles_cap = 0;
+    BatchTile *d_tiles = nullptr;
+    unsigned *d_misc = nullptr;              // [0] queue counter [1] rest count [2] kmin [3] kmax [4] nans
+    unsigned long long *d_nodes = nullptr;   // node count of the last build
+    void *pixels = nullptr;                  // input copy for host-side pixels
+    float *gval = nullptr;
+    unsigned long long *node = nullptr;
+    int *parent = nullptr;
+    unsigned char *isroot = nullptr;
+    void *attr_mem = nullptr;
+    AttrBufs attr;
+    unsigned rest_cap = 0;                   // graph runs: pointer-jumping capacity (0: not learned yet)
+    size_t rest_bytes = 0;
+    void *rest_mem = nullptr;
+    unsigned char *flag = nullptr;
+    int *target = nullptr;
+    float *filtered = nullptr;               // host-output staging
+    double *spectra = nullptr;
+    size_t spectra_cap = 0;
+    float *lvec = nullptr;                   // device lambda vectors (lvec1 then lvec2)
+    size_t lvec_cap = 0;
+    double *adj_acc = nullptr;
+    float *adj_io = nullptr;                 // host-side adjoint staging: v, then grad
+    double *adj_w = nullptr;
+    size_t adj_w_cap = 0;
+    // last run
+    bool valid = false;
+    dcf_op_set ops{};
+    // recorded graphs, one per distinct run configuration (a forward with outputs
+    // and a recomputation without them alternate in training), least recently used
+    // dropped beyond MAX_GRAPHS
+    struct Graph {
+        BatchKey key;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        uint64_t kernels = 0, used = 0;
+    };
+    static constexpr size_t MAX_GRAPHS = 4;
+    std::vector<Graph> graphs;
+    uint64_t uses = 0;
+    uint64_t graph_kernels = 0;              // kernel nodes of the last graph launched
+};
+
+static void batch_drop_graph(dcf_batch *b)
+{
+    for (auto &g : b->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+    }
+    b->graphs.clear();
+}
+
+static TreeView batch_view(const dcf_batch *b)
+{
+    TreeView v;
+    v.g = Geom{};
+    v.g.W = (int)b->N;  // unused by the node-parallel passes
+    v.g.H = v.g.D = 1;
+    v.g.WH = v.g.N = b->N;
+    v.g.conn = b->conn;
+    v.g.tw = b->tw;
+    v.g.th = b->th;
+    v.g.td = 1;
+    v.g.level_sync = 1;
+    v.tree_min = false;
+    v.kmax = b->d_misc + 3;
+    v.gval = b->gval;
+    v.parent = b->parent;
+    v.isroot = b->isroot;
+    for (int i = 0; i < 3; i++) v.pixdim[i] = b->pixdim[i];
+    v.integer_levels = b->dtype == U8 || b->dtype == U16;
+    return v;
+}
+
+static dcf_status batch_set_tiles(dcf_ctx *ctx, dcf_batch *b, int tw, int th, int ctas, int chunk)
+{
+    if (tw < 1 || th < 1 || tw * th > TILE_MAX_PIX)
+        return set_err(ctx, DCF_ERR_INVALID, "tile %dx%d (at most %d pixels)", tw, th, TILE_MAX_PIX);
+    const int maxc = batch_max_ctas_per_sm(b->dtype, tw, th);
+    if (maxc < 1) return set_err(ctx, DCF_ERR_INVALID, "tile %dx%d does not fit on an SM", tw, th);
+    if (ctas < 1 || ctas > maxc) ctas = maxc;
+    if (chunk < 1) chunk = 1;
+    std::vector<BatchTile> tl;
+    for (int i = 0; i < b->count; i++)
+        for (int y = 0; y < b->imgs[i].H; y += th)
+            for (int x = 0; x < b->imgs[i].W; x += tw) tl.push_back(BatchTile{i, x, y});
+    if (tl.size() > b->tiles_cap) {
+        if (b->d_tiles) CU(cudaFree(b->d_tiles));
+        b->d_tiles = nullptr;
+        b->tiles_cap = 0;
+        CU(cudaMalloc(&b->d_tiles, tl.size() * sizeof(BatchTile)));
+        b->tiles_cap = tl.size();
+    }
+    CU(cudaMemcpyAsync(b->d_tiles, tl.data(), tl.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    b->ntiles = (int)tl.size();
+    b->tw = tw;
+    b->th = th;
+    b->ctas = ctas;
+    b->chunk = chunk;
+    batch_drop_graph(b);
+    return DCF_OK;
+}
+
+static dcf_status batch_ensure_rest(dcf_ctx *ctx, dcf_batch *b, unsigned R)
+{
+    const size_t need = attr_rest_bytes(b->group, R);
+    if (need <= b->rest_bytes) return DCF_OK;
+    batch_drop_graph(b);
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (b->rest_mem) CU(cudaFree(b->rest_mem));
+    b->rest_mem = nullptr;
+    b->rest_bytes = 0;
+    CU(cudaMalloc(&b->rest_mem, need));
+    b->rest_bytes = need;
+    return DCF_OK;
+}
+
+// Enqueue the build + attributes (+ filter, + spectra) of every cutout.  graph:
+// the pointer-jumping phase uses the fixed capacity; otherwise the rest count is
+// read back (a host synchronisation) and the scratch sized from it.
+static dcf_status batch_forward(dcf_ctx *ctx, dcf_batch *b, const void *px, float *filtered, double *spectra,
+                                bool graph)
+{
+    cudaStream_t s = ctx->stream;
+    const int sm = ctx->sm_count;
+    const TreeView v = batch_view(b);
+    CU(cudaMemsetAsync(b->d_misc + 2, 0xFF, sizeof(unsigned), s));
+    CU(cudaMemsetAsync(b->d_misc + 3, 0, 2 * sizeof(unsigned), s));
+    CU(cudaMemsetAsync(b->d_nodes, 0, sizeof(unsigned long long), s));
+    launch_stats(b->dtype, px, b->N, b->d_misc + 2, b->d_misc + 3, b->d_misc + 4, sm, s);
+    launch_batch_build(b->dtype, px, v.g, b->d_imgs, b->d_tiles, b->ntiles, b->chunk, b->d_misc, b->gval, b->node,
+                       b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, sm, s);
+    CU(attr_zero(b->attr, (size_t)b->N, b->attr_mem, sm, s));
+    launch_batch_attr_pixels(v.g, b->d_imgs, b->d_tiles, b->ntiles, b->gval, b->parent, b->isroot, b->attr, sm, s);
+    unsigned *count = b->d_misc + 1;
+    launch_attributes_up(v, b->attr, count, ctx->up_steps, ctx->d_err, sm, s);
+    if (graph) {
+        launch_attributes_rest_cap(v, b->attr, b->rest_cap, count, b->rest_mem, ctx->d_err, sm, s);
+    } else {
+        dcf_status st = check_launch(ctx, 12);
+        if (st != DCF_OK) return st;
+        unsigned R = 0;
+        CU(cudaMemcpyAsync(&R, count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        if (R > 0) {
+            if ((st = batch_ensure_rest(ctx, b, R)) != DCF_OK) return st;
+            launch_attributes_rest(v, b->attr, R, count, b->rest_mem, ctx->d_err, sm, s);
+        }
+        // capacity of later graph runs: twice what this input needed
+        unsigned cap = R < (1u << 15) ? (1u << 16) : 2 * R;
+        if (cap > b->rest_cap) b->rest_cap = cap;
+    }
+    const dcf_op_set &o = b->ops;
+    if (o.filter_attr >= 0) {
+        FilterWork w{};
+        w.flag = b->flag;
+        w.target = b->target;
+        if (filtered)
+            launch_filter(v, b->attr, o.filter_attr, DCF_RULE_DIRECT, o.lambda, false, filtered, w, b->N, ctx->d_err,
+                          sm, s);
+        else
+            launch_direct_targets(v, b->attr, o.filter_attr, o.lambda, w, ctx->d_err, sm, s);
+    }
+    if (o.spec_attr1 >= 0 && spectra) {
+        CU(cudaMemsetAsync(spectra, 0, (size_t)b->count * o.n1 * o.n2 * 8, s));
+        launch_batch_spectrum(v.g, b->d_imgs, b->d_tiles, b->ntiles, b->parent, b->isroot, b->gval, b->attr,
+                              o.spec_attr1, b->lvec, o.n1, o.spec_attr2 == 0 ? -1 : o.spec_attr2, b->lvec + o.n1,
+                              o.n2, b->pixdim, spectra, sm, s);
+    }
+    return check_launch(ctx, 6);
+}
+
+// device error bits and NaN count after a run; *capacity: the graph's
+// pointer-jumping list overflowed
+static dcf_status batch_check(dcf_ctx *ctx, dcf_batch *b, bool *capacity)
+{
+    CU(cudaStreamSynchronize(ctx->stream));
+    unsigned err = 0, misc[5];
+    CU(cudaMemcpy(&err, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(misc, b->d_misc, sizeof(misc), cudaMemcpyDeviceToHost));
+    if (capacity) *capacity = (err & DEVERR_CAPACITY) != 0;
+    if (err) CU(cudaMemset(ctx->d_err, 0, sizeof(unsigned)));
+    if (capacity && *capacity) {
+        // the truncated list also trips the pointer-jumping link check; the run is
+        // redone without the graph, which reports any genuine error
+        err = 0;
+        const unsigned R = misc[1];
+        b->rest_cap = R > b->rest_cap ? 2 * R : 2 * b->rest_cap;
+    }
+    if (err) return set_err(ctx, DCF_ERR_TIMEOUT, "device loop bound exceeded (bits 0x%x)", err);
+    if (misc[4]) return set_err(ctx, DCF_ERR_NAN, "batch holds %u NaN values", misc[4]);
+    return DCF_OK;
+}
+
+static int spec_rule_error(dcf_ctx *ctx, int group, int a1, int a2, int n1, int n2, const float *l1, const float *l2)
+{
+    if (a1 < 0) return DCF_OK;
+    if (a1 >= DCF_NUM_ATTRIBUTES || (a1 != 0 && ATTR_GROUP[a1] != group))
+        return set_err(ctx, DCF_ERR_INVALID, "spectrum attribute %d is not in the batch's group", a1);
+    if (a1 == 0 && a2 != 0) return set_err(ctx, DCF_ERR_INVALID, "the attribute with the highest index must come first");
+    if (a2 != 0 && (a2 < 0 || a2 >= DCF_NUM_ATTRIBUTES || ATTR_GROUP[a2] != group))
+        return set_err(ctx, DCF_ERR_INVALID, "both 2-D spectrum attributes must be in one group");
+    if (n1 < 1 || n2 < 1 || !l1 || !l2) return set_err(ctx, DCF_ERR_INVALID, "bad lambda vectors");
+    return DCF_OK;
+}
+
+extern "C" {
+
+dcf_status dcf_batch_create(dcf_ctx *ctx, int count, const uint32_t *widths, const uint32_t *heights, int dtype,
+                            int connectivity, int attr_idx, const float *pixdim, dcf_batch **out)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !out || !widths || !heights) return DCF_ERR_INVALID;
+    *out = nullptr;
+    if (count < 1) return set_err(ctx, DCF_ERR_INVALID, "empty batch");
+    if (dtype < DCF_U8 || dtype > DCF_F32) return set_err(ctx, DCF_ERR_INVALID, "bad dtype %d", dtype);
+    if (connectivity != 4 && connectivity != 8)
+        return set_err(ctx, DCF_ERR_INVALID, "batch connectivity must be 4 or 8 (got %d)", connectivity);
+    if (attr_idx < 0 || attr_idx >= DCF_NUM_ATTRIBUTES) return set_err(ctx, DCF_ERR_INVALID, "bad attribute %d", attr_idx);
+    dcf_batch *b = new (std::nothrow) dcf_batch();
+    if (!b) return DCF_ERR_NOMEM;
+    b->ctx = ctx;
+    b->count = count;
+    b->dtype = dtype;
+    b->conn = connectivity;
+    b->attr_idx = attr_idx;
+    b->group = ATTR_GROUP[attr_idx];
+    if (pixdim)
+        for (int i = 0; i < 3; i++) b->pixdim[i] = pixdim[i];
+    std::vector<long long> offs(count);
+    long long N = 0;
+    b->imgs.resize(count);
+    for (int i = 0; i < count; i++) {
+        if (widths[i] < 1 || heights[i] < 1 || widths[i] > 0x7FFFFFFF || heights[i] > 0x7FFFFFFF) {
+            delete b;
+            return set_err(ctx, DCF_ERR_INVALID, "cutout %d is empty or too large", i);
+        }
+        offs[i] = N;
+        b->imgs[i] = BatchImg{N, (int)widths[i], (int)heights[i]};
+        N += (long long)widths[i] * heights[i];
+        if (N >= 0x7FFFFFFFLL) {
+            delete b;
+            return set_err(ctx, DCF_ERR_INVALID, "batch too large (limit 2^31-1 pixels)");
+        }
+    }
+    b->N = N;
+    static const size_t esize[4] = {1, 2, 4, 4};
+    dcf_status st = DCF_OK;
+#define BTRY(call)                                                                                            \
+    do {                                                                                                      \
+        cudaError_t _e = (call);                                                                              \
+        if (_e != cudaSuccess) {                                                                              \
+            st = set_err(ctx, _e == cudaErrorMemoryAllocation ? DCF_ERR_NOMEM : DCF_ERR_CUDA, "%s: %s", #call, \
+                         cudaGetErrorString(_e));                                                             \
+            goto fail;                                                                                        \
+        }                                                                                                     \
+    } while (0)
+    BTRY(cudaMalloc(&b->d_imgs, count * sizeof(BatchImg)));
+    BTRY(cudaMalloc(&b->d_offs, count * sizeof(long long)));
+    BTRY(cudaMalloc(&b->d_misc, 8 * sizeof(unsigned) + sizeof(unsigned long long)));
+    b->d_nodes = (unsigned long long *)(b->d_misc + 8);
+    BTRY(cudaMalloc(&b->pixels, (size_t)N * esize[dtype]));
+    BTRY(cudaMalloc(&b->gval, (size_t)N * 4));
+    BTRY(cudaMalloc(&b->node, (size_t)N * 8));
+    BTRY(cudaMalloc(&b->parent, (size_t)N * 4));
+    BTRY(cudaMalloc(&b->isroot, (size_t)N));
+    BTRY(cudaMalloc(&b->attr_mem, attr_bytes(b->group, (size_t)N)));
+    attr_carve(b->attr, b->group, dtype == U8 || dtype == U16, false, (size_t)N, b->attr_mem);
+    BTRY(cudaMemcpy(b->d_imgs, b->imgs.data(), count * sizeof(BatchImg), cudaMemcpyHostToDevice));
+    BTRY(cudaMemcpy(b->d_offs, offs.data(), count * sizeof(long long), cudaMemcpyHostToDevice));
+    BTRY(cudaMemset(b->d_misc, 0, 8 * sizeof(unsigned) + sizeof(unsigned long long)));
+    if ((st = batch_set_tiles(ctx, b, 64, 64, 0, 1)) != DCF_OK) goto fail;
+    *out = b;
+    return DCF_OK;
+fail:
+    dcf_batch_destroy(b);
+    return st;
+#undef BTRY
+}
+
+dcf_status dcf_batch_destroy(dcf_batch *b)
+{
+    if (!b) return DCF_ERR_INVALID;
+    if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+    batch_drop_graph(b);
+    void *bufs[] = {b->d_imgs, b->d_offs, b->d_tiles, b->d_misc, b->pixels, b->gval, b->node, b->parent, b->isroot,
+                    b->attr_mem, b->rest_mem, b->flag, b->target, b->filtered, b->spectra, b->lvec, b->adj_acc,
+                    b->adj_io, b->adj_w};
+    for (void *p : bufs)
+        if (p) cudaFree(p);
+    delete b;
+    return DCF_OK;
+}
+
+dcf_status dcf_batch_info(const dcf_batch *b, uint64_t *total_pixels, uint64_t *num_nodes, int *schedule,
+                          uint64_t *graph_kernels)
+{
+    if (!b) return DCF_ERR_INVALID;
+    if (total_pixels) *total_pixels = (uint64_t)b->N;
+    if (num_nodes) {
+        unsigned long long n = 0;
+        if (b->valid) {
+            cudaStreamSynchronize(b->ctx->stream);
+            cudaMemcpy(&n, b->d_nodes, sizeof(n), cudaMemcpyDeviceToHost);
+        }
+        *num_nodes = n;
+    }
+    if (schedule) {
+        schedule[0] = b->tw;
+        schedule[1] = b->th;
+        schedule[2] = b->ctas;
+        schedule[3] = b->chunk;
+    }
+    if (graph_kernels) *graph_kernels = b->graph_kernels;
+    return DCF_OK;
+}
+
+dcf_status dcf_batch_set_schedule(dcf_ctx *ctx, dcf_batch *b, int tile_w, int tile_h, int ctas_per_sm, int chunk)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !b) return DCF_ERR_INVALID;
+    return batch_set_tiles(ctx, b, tile_w, tile_h, ctas_per_sm, chunk);
+}
+
+dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *b, const void *pixels, int on_device, int repeats,
+                              double *best_ms)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !b || !pixels) return DCF_ERR_INVALID;
+    if (repeats < 1) repeats = 1;
+    static const size_t esize[4] = {1, 2, 4, 4};
+    const void *px = pixels;
+    if (!on_device) {
+        CU(cudaMemcpyAsync(b->pixels, pixels, (size_t)b->N * esize[b->dtype], cudaMemcpyHostToDevice, ctx->stream));
+        px = b->pixels;
+    }
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    const bool prof = ctx->prof_on;
+    ctx->prof_on = false;
+    // time the build phase (queue reset, persistent tile kernel, seams, canonical form)
+    auto time_build = [&](double *ms) -> dcf_status {
+        const TreeView v = batch_view(b);
+        std::vector<float> t;
+        for (int r = 0; r <= repeats; r++) {  // the first pass warms up
+            cudaEventRecord(e0, ctx->stream);
+            launch_batch_build(b->dtype, px, v.g, b->d_imgs, b->d_tiles, b->ntiles, b->chunk, b->d_misc, b->gval,
+                               b->node, b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, ctx->sm_count,
+                               ctx->stream);
+            cudaEventRecord(e1, ctx->stream);
+            dcf_status st = check_launch(ctx, 4);
+            if (st != DCF_OK) return st;
+            CU(cudaEventSynchronize(e1));
+            float x = 0.f;
+            cudaEventElapsedTime(&x, e0, e1);
+            if (r) t.push_back(x);
+        }
+        std::sort(t.begin(), t.end());
+        *ms = t[t.size() / 2];
+        return DCF_OK;
+    };
+    struct Cand {
+        int tw, th, ctas, chunk;
+    };
+    static const int shapes[][2] = {{64, 64}, {128, 32}, {32, 128}, {64, 32}, {32, 64}, {32, 32}, {128, 16}, {16, 64}};
+    Cand best{64, 64, 0, 1};
+    double best_t = 1e30;
+    dcf_status st = DCF_OK;
+    // 1) tile shape at full occupancy, 2) CTAs per SM and queue chunk for that shape
+    for (auto &sh : shapes) {
+        double ms;
+        if ((st = batch_set_tiles(ctx, b, sh[0], sh[1], 0, 1)) != DCF_OK) break;
+        if ((st = time_build(&ms)) != DCF_OK) break;
+        if (ms < best_t) {
+            best_t = ms;
+            best = Cand{sh[0], sh[1], b->ctas, 1};
+        }
+    }
+    if (st == DCF_OK) {
+        const int maxc = batch_max_ctas_per_sm(b->dtype, best.tw, best.th);
+        for (int c : {1, 2, 4, 8})
+            for (int ch : {1, 4}) {
+                if (c > maxc || (c == best.ctas && ch == 1)) continue;
+                double ms;
+                if ((st = batch_set_tiles(ctx, b, best.tw, best.th, c, ch)) != DCF_OK) break;
+                if ((st = time_build(&ms)) != DCF_OK) break;
+                if (ms < best_t) {
+                    best_t = ms;
+                    best = Cand{best.tw, best.th, c, ch};
+                }
+            }
+    }
+    ctx->prof_on = prof;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != DCF_OK) return st;
+    if ((st = batch_set_tiles(ctx, b, best.tw, best.th, best.ctas, best.chunk)) != DCF_OK) return st;
+    b->valid = false;  // the timed builds left no attributes
+    if (best_ms) *best_ms = best_t;
+    return batch_check(ctx, b, nullptr);
+}
+
+dcf_status dcf_batch_run(dcf_ctx *ctx, dcf_batch *b, const void *pixels, int pixels_on_device, const dcf_op_set *ops,
+                         float *filtered, double *spectra, int outputs_on_device)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !b || !pixels || !ops) return DCF_ERR_INVALID;
+    dcf_op_set o = *ops;
+    if (o.filter_attr >= DCF_NUM_ATTRIBUTES || (o.filter_attr > 0 && ATTR_GROUP[o.filter_attr] != b->group))
+        return set_err(ctx, DCF_ERR_INVALID, "filter attribute %d is not in the batch's group", o.filter_attr);
+    if (o.filter_attr < 0) o.filter_attr = -1;
+    if (o.spec_attr1 < 0) {
+        o.spec_attr1 = -1;
+        o.n1 = o.n2 = 0;
+    }
+    dcf_status st = (dcf_status)spec_rule_error(ctx, b->group, o.spec_attr1, o.spec_attr2, o.n1, o.n2, o.lvec1, o.lvec2);
+    if (st != DCF_OK) return st;
+    static const size_t esize[4] = {1, 2, 4, 4};
+    const size_t N = (size_t)b->N;
+    cudaStream_t s = ctx->stream;
+    // buffers the requested operations need (allocated once)
+    if (o.filter_attr >= 0 && !b->flag) {
+        CU(cudaMalloc(&b->flag, N));
+        CU(cudaMalloc(&b->target, N * 4));
+    }
+    if (filtered && !outputs_on_device && !b->filtered) CU(cudaMalloc(&b->filtered, N * 4));
+    const size_t nspec = o.spec_attr1 >= 0 ? (size_t)b->count * o.n1 * o.n2 : 0;
+    if (spectra && nspec && !outputs_on_device && nspec > b->spectra_cap) {
+        batch_drop_graph(b);
+        if (b->spectra) CU(cudaFree(b->spectra));
+        b->spectra = nullptr;
+        b->spectra_cap = 0;
+        CU(cudaMalloc(&b->spectra, nspec * 8));
+        b->spectra_cap = nspec;
+    }
+    if (o.spec_attr1 >= 0) {
+        if ((size_t)(o.n1 + o.n2) > b->lvec_cap) {
+            batch_drop_graph(b);
+            if (b->lvec) CU(cudaFree(b->lvec));
+            b->lvec = nullptr;
+            b->lvec_cap = 0;
+            CU(cudaMalloc(&b->lvec, (size_t)(o.n1 + o.n2) * 4));
+            b->lvec_cap = o.n1 + o.n2;
+        }
+        CU(cudaMemcpyAsync(b->lvec, o.lvec1, (size_t)o.n1 * 4, cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(b->lvec + o.n1, o.lvec2, (size_t)o.n2 * 4, cudaMemcpyHostToDevice, s));
+    }
+    const void *px = pixels;
+    if (!pixels_on_device) {
+        CU(cudaMemcpyAsync(b->pixels, pixels, N * esize[b->dtype], cudaMemcpyHostToDevice, s));
+        px = b->pixels;
+    }
+    float *d_filt = filtered ? (outputs_on_device ? filtered : b->filtered) : nullptr;
+    double *d_spec = (spectra && nspec) ? (outputs_on_device ? spectra : b->spectra) : nullptr;
+    b->ops = o;
+    b->valid = false;
+    bool capacity = false;
+    if (o.use_graph && b->rest_cap > 0) {
+        if ((st = batch_ensure_rest(ctx, b, b->rest_cap)) != DCF_OK) return st;
+        BatchKey k;
+        k.pixels = px;
+        k.filtered = d_filt;
+        k.spectra = d_spec;
+        k.filter_attr = o.filter_attr;
+        k.lambda = o.lambda;
+        k.a1 = o.spec_attr1;
+        k.a2 = o.spec_attr2;
+        k.n1 = o.n1;
+        k.n2 = o.n2;
+        k.tw = b->tw;
+        k.th = b->th;
+        k.ctas = b->ctas;
+        k.chunk = b->chunk;
+        k.cap = b->rest_cap;
+        k.rest_mem = b->rest_mem;
+        dcf_batch::Graph *gr = nullptr;
+        for (auto &g : b->graphs)
+            if (g.key == k) gr = &g;
+        if (!gr) {
+            if (b->graphs.size() >= dcf_batch::MAX_GRAPHS) {
+                auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
+                                            [](const dcf_batch::Graph &x, const dcf_batch::Graph &y) { return x.used < y.used; });
+                cudaGraphExecDestroy(lru->exec);
+                cudaGraphDestroy(lru->graph);
+                b->graphs.erase(lru);
+            }
+            const bool prof = ctx->prof_on;
+            ctx->prof_on = false;  // no timing events inside the recorded graph
+            const uint64_t launches0 = ctx->launches;
+            CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            dcf_status fst = batch_forward(ctx, b, px, d_filt, d_spec, true);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(s, &g);
+            ctx->prof_on = prof;
+            ctx->launches = launches0;
+            if (fst != DCF_OK) {
+                if (g) cudaGraphDestroy(g);
+                return fst;
+            }
+            if (ce != cudaSuccess) return set_err(ctx, DCF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+            dcf_batch::Graph ng;
+            ng.key = k;
+            ng.graph = g;
+            cudaError_t ie = cudaGraphInstantiate(&ng.exec, g, 0);
+            if (ie != cudaSuccess) {
+                cudaGraphDestroy(g);
+                return set_err(ctx, DCF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+            }
+            size_t nn = 0;
+            CU(cudaGraphGetNodes(g, nullptr, &nn));
+            std::vector<cudaGraphNode_t> nodes(nn);
+            CU(cudaGraphGetNodes(g, nodes.data(), &nn));
+            for (auto nd : nodes) {
+                cudaGraphNodeType ty;
+                if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ng.kernels++;
+            }
+            b->graphs.push_back(ng);
+            gr = &b->graphs.back();
+        }
+        gr->used = ++b->uses;
+        prof_begin(P_BATCH, s);
+        CU(cudaGraphLaunch(gr->exec, s));
+        prof_end(P_BATCH, s);
+        b->graph_kernels = gr->kernels;
+        ctx->launches += gr->kernels;
+        st = batch_check(ctx, b, &capacity);
+        if (st != DCF_OK) return st;
+    }
+    if (!o.use_graph || b->rest_cap == 0 || capacity) {
+        prof_begin(P_BATCH, s);
+        st = batch_forward(ctx, b, px, d_filt, d_spec, false);
+        prof_end(P_BATCH, s);
+        if (st != DCF_OK) return st;
+        st = batch_check(ctx, b, nullptr);
+        if (st != DCF_OK) return st;
+    }
+    b->valid = true;
+    if (!outputs_on_device) {
+        if (filtered) CU(cudaMemcpyAsync(filtered, d_filt, N * 4, cudaMemcpyDeviceToHost, s));
+        if (d_spec) CU(cudaMemcpyAsync(spectra, d_spec, nspec * 8, cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+    }
+    return DCF_OK;
+}
+
+__global__ void k_batch_local_parent(long long n, const int *__restrict__ parent, const long long *__restrict__ offs,
+                                     int count, long long *out)
+{
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+         p += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = count - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (offs[mid] <= p) lo = mid;
+            else hi = mid - 1;
+        }
+        const int q = parent[p];
+        out[p] = q < 0 ? -1 : q - offs[lo];
+    }
+}
+
+dcf_status dcf_batch_parent(dcf_ctx *ctx, dcf_batch *b, int64_t *parent, int on_device)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !b || !parent) return DCF_ERR_INVALID;
+    if (!b->valid) return set_err(ctx, DCF_ERR_STATE, "the batch has not been run");
+    const size_t N = (size_t)b->N;
+    long long *dst = (long long *)parent;
+    void *sbuf = nullptr;
+    dcf_status st;
+    if (!on_device) {
+        if ((st = scratch(ctx, 10, N * 8, &sbuf)) != DCF_OK) return st;
+        dst = (long long *)sbuf;
+    }
+    k_batch_local_parent<<<grid_for(b->N, 256, ctx->sm_count), 256, 0, ctx->stream>>>(b->N, b->parent, b->d_offs,
+                                                                                      b->count, dst);
+    if ((st = check_launch(ctx, 1)) != DCF_OK) return st;
+    if (!on_device) CU(cudaMemcpyAsync(parent, dst, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+dcf_status dcf_batch_node_attribute(dcf_ctx *ctx, dcf_batch *b, int attr_idx, double *out, int on_device)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !b || !out) return DCF_ERR_INVALID;
+    if (!b->valid) return set_err(ctx, DCF_ERR_STATE, "the batch has not been run");
+    if (attr_idx < 0 || attr_idx >= DCF_NUM_ATTRIBUTES || (attr_idx != 0 && ATTR_GROUP[attr_idx] != b->group))
+        return set_err(ctx, DCF_ERR_INVALID, "attribute %d is not in the batch's group", attr_idx);
+    const size_t N = (size_t)b->N;
+    double *dst = out;
+    dcf_status st;
+    if (!on_device) {
+        void *sbuf;
+        if ((st = scratch(ctx, 10, N * 8, &sbuf)) != DCF_OK) return st;
+        dst = (double *)sbuf;
+    }
+    launch_node_attr(batch_view(b), b->attr, attr_idx, false, dst, ctx->sm_count, ctx->stream);
+    if ((st = check_launch(ctx, 1)) != DCF_OK) return st;
+    if (!on_device) CU(cudaMemcpyAsync(out, dst, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+dcf_status dcf_batch_adjoint(dcf_ctx *ctx, dcf_batch *b, const float *grad_filtered, const double *grad_spectra,
+                             float *grad_pixels, int on_device)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !b || !grad_pixels) return DCF_ERR_INVALID;
+    if (!b->valid) return set_err(ctx, DCF_ERR_STATE, "the batch has not been run");
+    if (b->dtype != F32) return set_err(ctx, DCF_ERR_UNSUPPORTED, "the adjoint needs float32 pixels");
+    const dcf_op_set &o = b->ops;
+    if (grad_filtered && o.filter_attr < 0) return set_err(ctx, DCF_ERR_STATE, "the last run had no filter");
+    if (grad_spectra && o.spec_attr1 < 0) return set_err(ctx, DCF_ERR_STATE, "the last run had no spectrum");
+    const size_t N = (size_t)b->N;
+    const size_t nspec = (size_t)b->count * o.n1 * o.n2;
+    cudaStream_t s = ctx->stream;
+    if (!b->adj_acc) CU(cudaMalloc(&b->adj_acc, N * 8));
+    const float *v = grad_filtered;
+    const double *w = grad_spectra;
+    float *grad = grad_pixels;
+    if (!on_device) {
+        if (!b->adj_io) CU(cudaMalloc(&b->adj_io, N * 8));
+        if (grad_filtered) {
+            CU(cudaMemcpyAsync(b->adj_io, grad_filtered, N * 4, cudaMemcpyHostToDevice, s));
+            v = b->adj_io;
+        }
+        if (grad_spectra) {
+            if (nspec > b->adj_w_cap) {
+                if (b->adj_w) CU(cudaFree(b->adj_w));
+                b->adj_w = nullptr;
+                b->adj_w_cap = 0;
+                CU(cudaMalloc(&b->adj_w, nspec * 8));
+                b->adj_w_cap = nspec;
+            }
+            CU(cudaMemcpyAsync(b->adj_w, grad_spectra, nspec * 8, cudaMemcpyHostToDevice, s));
+            w = b->adj_w;
+        }
+        grad = b->adj_io + N;
+    }
+    CU(cudaMemsetAsync(b->adj_acc, 0, N * 8, s));
+    AdjointArgs j;
+    j.target = grad_filtered ? b->target : nullptr;
+    j.v = v;
+    j.w = grad_spectra ? w : nullptr;
+    j.a1 = o.spec_attr1;
+    j.n1 = o.n1;
+    j.a2 = o.spec_attr2 == 0 ? -1 : o.spec_attr2;
+    j.n2 = o.n2;
+    j.l1 = b->lvec;
+    j.l2 = b->lvec ? b->lvec + o.n1 : nullptr;
+    j.offs = b->d_offs;
+    j.count = b->count;
+    j.acc = b->adj_acc;
+    j.grad = grad;
+    launch_adjoint(batch_view(b), b->attr, j, ctx->sm_count, s);
+    dcf_status st = check_launch(ctx, 2);
+    if (st != DCF_OK) return st;
+    if (!on_device) CU(cudaMemcpyAsync(grad_pixels, grad, N * 4, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(ctx);
+}
+
+dcf_status dcf_tree_adjoint(dcf_ctx *ctx, dcf_tree *t, const dcf_op_set *ops, const float *grad_filtered,
+                            const double *grad_spectrum, float *grad_pixels, int on_device)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !t || !ops || !grad_pixels) return DCF_ERR_INVALID;
+    if (t->dtype != F32 || t->tree_min)
+        return set_err(ctx, DCF_ERR_UNSUPPORTED, "the adjoint needs a max-tree of float32 pixels");
+    const dcf_op_set &o = *ops;
+    if (grad_filtered) {
+        dcf_status st = check_attr(ctx, t, o.filter_attr);
+        if (st != DCF_OK) return st;
+    }
+    if (grad_spectrum) {
+        dcf_status st = check_attr(ctx, t, o.spec_attr1);
+        if (st != DCF_OK) return st;
+        st = (dcf_status)spec_rule_error(ctx, t->attr.group, o.spec_attr1, o.spec_attr2, o.n1, o.n2, o.lvec1, o.lvec2);
+        if (st != DCF_OK) return st;
+    }
+    const size_t N = (size_t)t->g.N;
+    const size_t nspec = grad_spectrum ? (size_t)o.n1 * o.n2 : 0;
+    cudaStream_t s = ctx->stream;
+    dcf_status st;
+    // scratch: 1 flag, 2 target, 10 accumulator, 11 lambda vectors + host-side staging
+    void *acc, *io;
+    const size_t lbytes = grad_spectrum ? ((size_t)(o.n1 + o.n2) * 4 + 255) / 256 * 256 : 0;
+    const size_t io_bytes = lbytes + (on_device ? 0 : nspec * 8 + N * 8);
+    if ((st = scratch(ctx, 10, N * 8, &acc)) != DCF_OK) return st;
+    if ((st = scratch(ctx, 11, io_bytes + 256, &io)) != DCF_OK) return st;
+    float *dl = (float *)io;
+    double *dw = (double *)((char *)io + lbytes);
+    float *dv = (float *)((char *)io + lbytes + nspec * 8);
+    float *dgrad = dv + N;
+    AdjointArgs j;
+    if (grad_filtered) {
+        FilterWork w{};
+        void *p;
+        if ((st = scratch(ctx, 1, N, &p)) != DCF_OK) return st;
+        w.flag = (unsigned char *)p;
+        if ((st = scratch(ctx, 2, N * 4, &p)) != DCF_OK) return st;
+        w.target = (int *)p;
+        launch_direct_targets(view_of(t), t->attr, o.filter_attr, o.lambda, w, ctx->d_err, ctx->sm_count, s);
+        j.target = w.target;
+        j.v = grad_filtered;
+        if (!on_device) {
+            CU(cudaMemcpyAsync(dv, grad_filtered, N * 4, cudaMemcpyHostToDevice, s));
+            j.v = dv;
+        }
+    }
+    if (grad_spectrum) {
+        CU(cudaMemcpyAsync(dl, o.lvec1, (size_t)o.n1 * 4, cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(dl + o.n1, o.lvec2, (size_t)o.n2 * 4, cudaMemcpyHostToDevice, s));
+        j.w = grad_spectrum;
+        if (!on_device) {
+            CU(cudaMemcpyAsync(dw, grad_spectrum, nspec * 8, cudaMemcpyHostToDevice, s));
+            j.w = dw;
+        }
+        j.a1 = o.spec_attr1;
+        j.n1 = o.n1;
+        j.a2 = o.spec_attr2 == 0 ? -1 : o.spec_attr2;
+        j.n2 = o.n2;
+        j.l1 = dl;
+        j.l2 = dl + o.n1;
+    }
+    static const long long zero_off = 0;
+    j.offs = &zero_off;  // not read with count == 1
+    j.count = 1;
+    j.acc = (double *)acc;
+    j.grad = on_device ? grad_pixels : dgrad;
+    CU(cudaMemsetAsync(acc, 0, N * 8, s));
+    launch_adjoint(view_of(t), t->attr, j, ctx->sm_count, s);
+    if ((st = check_launch(ctx, 4)) != DCF_OK) return st;
+    if (!on_device) CU(cudaMemcpyAsync(grad_pixels, dgrad, N * 4, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(ctx);
+}
+
+}  // extern "C"

@@ -166,8 +166,9 @@ __global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs 
 }
 
 // nodes left for the pointer-jumping phase, listed in any order
+// (list entries beyond cap are dropped and flagged: the caller sized the list)
 __global__ void k_collect_rest(long long n, const unsigned char *__restrict__ isroot, int *pending, int *list,
-                               unsigned *count)
+                               unsigned *count, unsigned cap, unsigned *err)
 {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
          p += (long long)gridDim.x * blockDim.x) {
@@ -175,9 +176,18 @@ __global__ void k_collect_rest(long long n, const unsigned char *__restrict__ is
         int s = pending[p];
         if (s > 0 || s == STALLED) {
             unsigned i = atomicAdd(count, 1u);
-            if (list) list[i] = (int)p;
+            if (list) {
+                if (i < cap) list[i] = (int)p;
+                else raise_error(err, DEVERR_CAPACITY);
+            }
         }
     }
+}
+
+__device__ __forceinline__ unsigned rest_count(const unsigned *count, unsigned cap)
+{
+    const unsigned c = *count;
+    return c < cap ? c : cap;
 }
 
 // Compact records of the remaining nodes: R-long arrays, one per field.
@@ -209,10 +219,11 @@ __device__ __forceinline__ void rest_copy(const RestRecs &dst, int i, const Attr
 }
 
 template <int G>
-__global__ void k_rest_gather(const int *__restrict__ list, const unsigned *count, const int *__restrict__ parent,
-                              int *pending, AttrBufs a, RestRecs r, int *jump, unsigned *err)
+__global__ void k_rest_gather(const int *__restrict__ list, const unsigned *count, unsigned cap,
+                              const int *__restrict__ parent, int *pending, AttrBufs a, RestRecs r, int *jump,
+                              unsigned *err)
 {
-    const unsigned R = *count;
+    const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
         rest_copy<G>(r, (int)i, a, list[i], true);
         pending[list[i]] = -(int)(i + 16);  // position of the node in the compact list
@@ -220,10 +231,10 @@ __global__ void k_rest_gather(const int *__restrict__ list, const unsigned *coun
 }
 
 template <int G>
-__global__ void k_rest_links(const int *__restrict__ list, const unsigned *count, const int *__restrict__ parent,
-                             const int *__restrict__ pending, int *jump, unsigned *err)
+__global__ void k_rest_links(const int *__restrict__ list, const unsigned *count, unsigned cap,
+                             const int *__restrict__ parent, const int *__restrict__ pending, int *jump, unsigned *err)
 {
-    const unsigned R = *count;
+    const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
         int q = parent[list[i]];
         int j = NONE;
@@ -240,10 +251,10 @@ __global__ void k_rest_links(const int *__restrict__ list, const unsigned *count
 // record into the node 2^k levels above it (sums; min/max for the bounding box).
 // Reads the `in` buffers, writes `out` (initialised as a copy of `in`).
 template <int G, bool EXACT>
-__global__ void k_jump_fold(const unsigned *count, const int *__restrict__ jin, int *jout, RestRecs in, RestRecs out,
-                            bool has_z)
+__global__ void k_jump_fold(const unsigned *count, unsigned cap, const int *__restrict__ jin, int *jout, RestRecs in,
+                            RestRecs out, bool has_z)
 {
-    const unsigned R = *count;
+    const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
         int j = jin[i];
         if (j == NONE) {
@@ -269,11 +280,27 @@ __global__ void k_jump_fold(const unsigned *count, const int *__restrict__ jin, 
 }
 
 template <int G>
-__global__ void k_rest_scatter(const int *__restrict__ list, const unsigned *count, AttrBufs a, RestRecs r)
+__global__ void k_rest_scatter(const int *__restrict__ list, const unsigned *count, unsigned cap, AttrBufs a,
+                               RestRecs r)
 {
-    const unsigned R = *count;
+    const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x)
         rest_copy<G>(r, (int)i, a, list[i], false);
+}
+
+// out = in over the first min(count, cap) records (device-side length)
+template <int G>
+__global__ void k_copy_recs(const unsigned *count, unsigned cap, RestRecs in, RestRecs out)
+{
+    const unsigned R = rest_count(count, cap);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
+        out.area[i] = in.area[i];
+        if (G == 1) for (int d = 0; d < 3; d++) { out.bmin[d][i] = in.bmin[d][i]; out.bmax[d][i] = in.bmax[d][i]; }
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) out.s1[d][i] = in.s1[d][i];
+        if (G == 4) for (int d = 0; d < 6; d++) out.s2[d][i] = in.s2[d][i];
+        if (G == 3 || G == 4)
+            for (int d = 0; d < 5; d++) ((unsigned long long *)out.gw[d])[i] = ((const unsigned long long *)in.gw[d])[i];
+    }
 }
 
 static size_t rest_record_bytes(int group)
@@ -318,39 +345,78 @@ static void copy_recs(const RestRecs &dst, const RestRecs &src, int group, size_
         if (dst.gw[d]) cudaMemcpyAsync(dst.gw[d], src.gw[d], 8 * R, cudaMemcpyDeviceToDevice, s);
 }
 
-void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_steps, unsigned *err, int sm,
-                       cudaStream_t s)
-{
-    int nb = grid_for(t.g.N, 256, sm);
-#define DCF_PIX(G, E) k_attr_pixels<G, E><<<nb, 256, 0, s>>>(t.gval, t.g, t.parent, t.isroot, a)
-    prof_begin(P_ATTR_PIX, s);
-    switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
-    case 0: case 1: DCF_PIX(0, false); break;
-    case 2: case 3: DCF_PIX(1, false); break;
-    case 4: case 5: DCF_PIX(2, false); break;
-    case 6: DCF_PIX(3, false); break;
-    case 7: DCF_PIX(3, true); break;
-    case 8: DCF_PIX(4, false); break;
-    default: DCF_PIX(4, true); break;
+#define DCF_GROUP_SWITCH(M)                                  \
+    switch (a.group * 2 + (a.exact_g ? 1 : 0)) {             \
+    case 0: case 1: M(0, false); break;                      \
+    case 2: case 3: M(1, false); break;                      \
+    case 4: case 5: M(2, false); break;                      \
+    case 6: M(3, false); break;                              \
+    case 7: M(3, true); break;                               \
+    case 8: M(4, false); break;                              \
+    default: M(4, true); break;                              \
     }
-#undef DCF_PIX
-    prof_end(P_ATTR_PIX, s);
+
+void launch_attributes_up(const TreeView &t, AttrBufs &a, unsigned *count, int up_steps, unsigned *err, int sm,
+                          cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_ATTR_UP, s);
     k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending);
 #define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, up_steps, err)
-    switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
-    case 0: case 1: DCF_UP(0, false); break;
-    case 2: case 3: DCF_UP(1, false); break;
-    case 4: case 5: DCF_UP(2, false); break;
-    case 6: DCF_UP(3, false); break;
-    case 7: DCF_UP(3, true); break;
-    case 8: DCF_UP(4, false); break;
-    default: DCF_UP(4, true); break;
-    }
+    DCF_GROUP_SWITCH(DCF_UP)
 #undef DCF_UP
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, nullptr, count);
+    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, nullptr, count, 0u, err);
     prof_end(P_ATTR_UP, s);
+}
+
+void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_steps, unsigned *err, int sm,
+                       cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+#define DCF_PIX(G, E) k_attr_pixels<G, E><<<nb, 256, 0, s>>>(t.gval, t.g, t.parent, t.isroot, a)
+    prof_begin(P_ATTR_PIX, s);
+    DCF_GROUP_SWITCH(DCF_PIX)
+#undef DCF_PIX
+    prof_end(P_ATTR_PIX, s);
+    launch_attributes_up(t, a, count, up_steps, err, sm, s);
+}
+
+// Pointer-jumping phase over the nodes the walkers left.  `cap` sizes the scratch;
+// exact == true: cap is the count the caller read back (round count from it, copies
+// by cudaMemcpyAsync of that length); exact == false: the count stays on the device,
+// rounds cover any forest of up to cap nodes and copies are kernels.
+template <int G, bool E>
+static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool exact, unsigned *count, void *scratch,
+                       unsigned *err, int sm, cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+    char *m = (char *)scratch;
+    int *list = (int *)m;
+    m += (4 * (size_t)cap + 255) / 256 * 256;
+    int *j0 = (int *)m;
+    m += (4 * (size_t)cap + 255) / 256 * 256;
+    int *j1 = (int *)m;
+    m += (4 * (size_t)cap + 255) / 256 * 256;
+    RestRecs r0 = carve(m, a.group, cap), r1 = carve(m, a.group, cap);
+    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, list, count, cap, err);
+    if (cap == 0) return;
+    const int rb = grid_for(cap, 256, sm);
+    k_rest_gather<G><<<rb, 256, 0, s>>>(list, count, cap, t.parent, a.pending, a, r0, j0, err);
+    k_rest_links<G><<<rb, 256, 0, s>>>(list, count, cap, t.parent, a.pending, j0, err);
+    int rounds = 0;
+    while ((1u << rounds) < cap && rounds < 31) rounds++;
+    RestRecs *ri = &r0, *ro = &r1;
+    int *ji = j0, *jo = j1;
+    for (int k = 0; k < rounds; k++) {
+        if (exact) copy_recs(*ro, *ri, G, cap, s);
+        else k_copy_recs<G><<<rb, 256, 0, s>>>(count, cap, *ri, *ro);
+        k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, cap, ji, jo, *ri, *ro, a.has_z);
+        RestRecs *tr = ri; ri = ro; ro = tr;
+        int *tj = ji; ji = jo; jo = tj;
+    }
+    k_rest_scatter<G><<<rb, 256, 0, s>>>(list, count, cap, a, *ri);
 }
 
 // Phase 2: R = number of nodes the walkers left (read back by the caller), scratch
@@ -358,47 +424,20 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_s
 void launch_attributes_rest(const TreeView &t, AttrBufs &a, unsigned R, unsigned *count, void *scratch,
                             unsigned *err, int sm, cudaStream_t s)
 {
-    const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_ATTR_REST, s);
-    char *m = (char *)scratch;
-    int *list = (int *)m;
-    m += (4 * (size_t)R + 255) / 256 * 256;
-    int *j0 = (int *)m;
-    m += (4 * (size_t)R + 255) / 256 * 256;
-    int *j1 = (int *)m;
-    m += (4 * (size_t)R + 255) / 256 * 256;
-    RestRecs r0 = carve(m, a.group, R), r1 = carve(m, a.group, R);
-    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, list, count);
-    if (R > 0) {
-        const int rb = grid_for(R, 256, sm);
-#define DCF_REST(G, E)                                                                           \
-    do {                                                                                         \
-        k_rest_gather<G><<<rb, 256, 0, s>>>(list, count, t.parent, a.pending, a, r0, j0, err);   \
-        k_rest_links<G><<<rb, 256, 0, s>>>(list, count, t.parent, a.pending, j0, err);          \
-        int rounds = 0;                                                                          \
-        while ((1u << rounds) < R && rounds < 31) rounds++;                                     \
-        RestRecs *ri = &r0, *ro = &r1;                                                           \
-        int *ji = j0, *jo = j1;                                                                  \
-        for (int k = 0; k < rounds; k++) {                                                       \
-            copy_recs(*ro, *ri, G, R, s);                                                        \
-            k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, ji, jo, *ri, *ro, a.has_z);                       \
-            RestRecs *tr = ri; ri = ro; ro = tr;                                                 \
-            int *tj = ji; ji = jo; jo = tj;                                                      \
-        }                                                                                        \
-        k_rest_scatter<G><<<rb, 256, 0, s>>>(list, count, a, *ri);                               \
-    } while (0)
-        switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
-        case 0: case 1: DCF_REST(0, false); break;
-        case 2: case 3: DCF_REST(1, false); break;
-        case 4: case 5: DCF_REST(2, false); break;
-        case 6: DCF_REST(3, false); break;
-        case 7: DCF_REST(3, true); break;
-        case 8: DCF_REST(4, false); break;
-        default: DCF_REST(4, true); break;
-        }
+#define DCF_REST(G, E) rest_phase<G, E>(t, a, R, true, count, scratch, err, sm, s)
+    DCF_GROUP_SWITCH(DCF_REST)
 #undef DCF_REST
-    }
+    prof_end(P_ATTR_REST, s);
+}
+
+void launch_attributes_rest_cap(const TreeView &t, AttrBufs &a, unsigned cap, unsigned *count, void *scratch,
+                                unsigned *err, int sm, cudaStream_t s)
+{
+    prof_begin(P_ATTR_REST, s);
+#define DCF_REST(G, E) rest_phase<G, E>(t, a, cap, false, count, scratch, err, sm, s)
+    DCF_GROUP_SWITCH(DCF_REST)
+#undef DCF_REST
     prof_end(P_ATTR_REST, s);
 }
 

@@ -13,7 +13,7 @@
 //   k_canon        flatten to the reference's canonical form (flood.c:127-141,
 //                  get_levelroot :693-712) into the int32 parent array: pixel ->
 //                  level root, root -> parent's level root; root flags; node count.
-#include "dcf_kernels.cuh"
+#include "dcf_tile.cuh"
 
 namespace dcf {
 
@@ -48,144 +48,6 @@ __global__ void k_stats(const T *__restrict__ img, long long n, unsigned *kmin, 
     }
 }
 
-// ---------------------------------------------------------------------------
-// tile build
-// ---------------------------------------------------------------------------
-struct SmemAcc {
-    unsigned long long *w;
-    unsigned *err;
-    int npix;
-    __device__ uint64_t load(int i) const { return ((volatile unsigned long long *)w)[i]; }
-    __device__ void store(int i, uint64_t v) { ((volatile unsigned long long *)w)[i] = v; }
-    __device__ bool cas(int i, uint64_t expect, uint64_t v) { return atomicCAS(w + i, expect, v) == expect; }
-    __device__ long long walk_bound() const { return npix + 1; }
-    __device__ void error(unsigned bit) { raise_error(err, bit); }
-};
-
-// Max-tree of one tile by the whole CTA.  The tile starts at (x0, y0, z0) of an
-// image of geometry g whose pixel (x, y, z) has global index off + z*WH + y*W + x
-// (off > 0 for one cutout of a batch).  smem holds tw*th*td node words followed by
-// the row stacks.  Writes gval and the tile forest (level-root form, global
-// indices) into gnode.
-template <typename T, bool MIN>
-__device__ __forceinline__ void build_tile(const T *__restrict__ img, long long off, const Geom &g, int x0, int y0,
-                                           int z0, float gmax, float *__restrict__ gval,
-                                           unsigned long long *__restrict__ gnode, unsigned *err,
-                                           unsigned long long *smem_tile)
-{
-    // tile extents from the geometry (at most 4096 pixels: local indices < 2^16)
-    const bool is3d = g.D > 1;
-    const int TW = g.tw, TH = g.th, TD = g.td, TILE_PIX = TW * TH * TD;
-    unsigned long long *snode = smem_tile;                               // TILE_PIX words
-    unsigned short *sstk = (unsigned short *)(smem_tile + TILE_PIX);     // one TW-long stack per row
-    const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
-    const int tid = threadIdx.x;
-
-    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
-        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
-        uint32_t k = 0;
-        if (lx < wl && ly < hl && lz < dl) {
-            long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
-            float lv = level_of<T, MIN>(img[gp], gmax);
-            gval[gp] = lv;
-            k = order_key(lv);
-        }
-        snode[i] = wmake(k, NONE);
-    }
-    __syncthreads();
-
-    // 1-D max-tree of each row with a stack (pop higher keys; the popped chain
-    // hangs off the next popped element, the last one off the new pixel).
-    const int nrows = TH * TD;
-    for (int r = tid; r < nrows; r += TILE_THREADS) {
-        int ly = r % TH, lz = r / TH;
-        if (ly >= hl || lz >= dl) continue;
-        unsigned short *stk = sstk + r * TW;
-        int sp = 0;
-        const int base = r * TW;
-        for (int lx = 0; lx < wl; lx++) {
-            int i = base + lx;
-            uint32_t ki = wkey(snode[i]);
-            int last = NONE;
-            while (sp > 0 && wkey(snode[stk[sp - 1]]) > ki) {
-                int t = stk[--sp];
-                if (last != NONE) snode[last] = wmake(wkey(snode[last]), t);
-                last = t;
-            }
-            if (last != NONE) snode[last] = wmake(wkey(snode[last]), i);
-            stk[sp++] = (unsigned short)i;
-        }
-        for (int j = sp - 1; j >= 1; j--) snode[stk[j]] = wmake(wkey(snode[stk[j]]), stk[j - 1]);
-    }
-    __syncthreads();
-
-    SmemAcc acc{snode, err, TILE_PIX};
-    const Offs offs = forward_offsets(g.conn);
-    // merge row bands along y (each z slice), then slabs along z; at level k the
-    // seams are the rows (slices) c with c % 2^(k+1) == 2^k
-    for (int axis = 1; axis <= (is3d ? 2 : 1); axis++) {
-        const int ext = axis == 1 ? TH : TD;
-        for (int half = 1; half < ext; half <<= 1) {
-            const int nseams = (ext + 2 * half - 1) / (2 * half);
-            const int other = axis == 1 ? TD : TH;  // slices (axis y) or rows (axis z)
-            // all edges across the seams of this level at once; correctness does not
-            // depend on the order (see connect)
-            const long long work = (long long)nseams * other * TW;
-            for (long long w = tid; w < work; w += TILE_THREADS) {
-                int lx = (int)(w % TW);
-                long long rest = w / TW;
-                int o = (int)(rest % other);
-                int s = (int)(rest / other);
-                int c = s * 2 * half + half;  // seam coordinate on the axis
-                int ly, lz;
-                if (axis == 1) { ly = c; lz = o; }
-                else { lz = c; ly = o; }
-                if (lx >= wl || ly >= hl || lz >= dl) continue;
-                int p = lx + ly * TW + lz * TW * TH;
-                // edges from p to the previous row / slice: the reversed forward offsets
-                for (int e = 0; e < offs.n; e++) {
-                    int dx = offs.d[e][0], dy = offs.d[e][1], dz = offs.d[e][2];
-                    bool crosses = axis == 1 ? (dz == 0 && dy == 1) : (dz == 1);
-                    if (!crosses) continue;
-                    int qx = lx - dx, qy = ly - dy, qz = lz - dz;
-                    if (qx < 0 || qx >= wl || qy < 0 || qy >= hl || qz < 0 || qz >= dl) continue;
-                    connect(acc, p, qx + qy * TW + qz * TW * TH, MERGE_BOUND_SMEM);
-                }
-            }
-            // levels are ordered for shorter merge walks, not for correctness:
-            // without the barrier warps run ahead into the next level
-            if (g.level_sync) __syncthreads();
-        }
-    }
-    __syncthreads();
-
-    // level-root form inside the tile (read-only walks, then each pixel writes its
-    // own word): pixel -> level root, root -> parent's level root; to global indices
-    unsigned short *sroot = sstk;  // the row stacks are no longer needed
-    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
-        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
-        sroot[i] = (lx < wl && ly < hl && lz < dl) ? (unsigned short)levelroot_ro(acc, i) : (unsigned short)0xFFFFu;
-    }
-    __syncthreads();
-    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
-        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
-        if (lx >= wl || ly >= hl || lz >= dl) continue;
-        const uint64_t w = snode[i];
-        int p = sroot[i];
-        if (p == i) {  // level root: its parent node's level root
-            const int q = wpar(w);
-            p = q == NONE ? NONE : (int)sroot[q];
-        }
-        int out = NONE;
-        if (p != NONE) {
-            int px = p % TW, py = (p / TW) % TH, pz = p / (TW * TH);
-            out = (int)(off + (long long)(z0 + pz) * g.WH + (long long)(y0 + py) * g.W + (x0 + px));
-        }
-        long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
-        gnode[gp] = wmake(wkey(w), out);
-    }
-}
-
 template <typename T, bool MIN>
 __global__ void __launch_bounds__(TILE_THREADS)
 k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__restrict__ gval,
@@ -200,17 +62,6 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
 // ---------------------------------------------------------------------------
 // seam merge in HBM
 // ---------------------------------------------------------------------------
-struct GlobalAcc {
-    unsigned long long *w;
-    unsigned *err;
-    long long n;
-    __device__ uint64_t load(int i) const { return ((volatile unsigned long long *)w)[i]; }
-    __device__ void store(int i, uint64_t v) { ((volatile unsigned long long *)w)[i] = v; }
-    __device__ bool cas(int i, uint64_t expect, uint64_t v) { return atomicCAS(w + i, expect, v) == expect; }
-    __device__ long long walk_bound() const { return n + 1; }
-    __device__ void error(unsigned bit) { raise_error(err, bit); }
-};
-
 // Seam merge: work item = (tile, face, segment).  Faces are the tile's +x, -x, +y,
 // -y, +z sides (forward offsets never point to -z); a segment is a run of face
 // pixels one thread walks in order, merging every forward edge of each pixel that
@@ -301,6 +152,14 @@ __global__ void k_canon(unsigned long long *gnode, Geom g, int *parent, unsigned
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
+void launch_canon(unsigned long long *node, const Geom &g, int *parent, unsigned char *isroot,
+                  unsigned long long *num_nodes, unsigned *err, int sm_count, cudaStream_t s)
+{
+    prof_begin(P_CANON, s);
+    k_canon<<<grid_for(g.N, 256, sm_count), 256, 0, s>>>(node, g, parent, isroot, num_nodes, err);
+    prof_end(P_CANON, s);
+}
+
 template <typename T, bool MIN>
 static void build_t(const BuildArgs &a, cudaStream_t s)
 {
@@ -318,10 +177,7 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
         k_seam_merge<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err);
     }
     prof_end(P_SEAM, s);
-    int nb = grid_for(a.g.N, 256, a.sm_count);
-    prof_begin(P_CANON, s);
-    k_canon<<<nb, 256, 0, s>>>(a.node, a.g, a.parent, a.isroot, a.num_nodes, a.err);
-    prof_end(P_CANON, s);
+    launch_canon(a.node, a.g, a.parent, a.isroot, a.num_nodes, a.err, a.sm_count, s);
 }
 
 void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsigned *kmax, unsigned *nans,

@@ -28,6 +28,7 @@ enum DevErr : unsigned {
     DEVERR_MERGE_BOUND = 1u << 0,   // a merge loop exceeded its iteration bound
     DEVERR_WALK_BOUND = 1u << 1,    // a tree walk exceeded its iteration bound
     DEVERR_WAIT_BOUND = 1u << 2,    // a bounded wait gave up (work queue / flag)
+    DEVERR_CAPACITY = 1u << 3,      // a fixed-capacity work list overflowed (results incomplete)
 };
 
 struct Geom {

@@ -46,6 +46,28 @@ struct BuildArgs {
 void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsigned *kmax, unsigned *nans,
                   int sm_count, cudaStream_t s);
 void launch_build(const BuildArgs &a, cudaStream_t s);
+// canonical form of the merged node words (pixel -> level root, root -> parent's level root)
+void launch_canon(unsigned long long *node, const Geom &g, int *parent, unsigned char *isroot,
+                  unsigned long long *num_nodes, unsigned *err, int sm_count, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// batches of 2-D cutouts: pixels of all cutouts concatenated, cutout i at element
+// off_i; trees use global indices, so the node-parallel passes run unchanged on
+// the concatenation
+// ---------------------------------------------------------------------------
+struct BatchImg {
+    long long off;
+    int W, H;
+};
+struct BatchTile {
+    int img, x0, y0;
+};
+// persistent work-queue tile build (grid = sm_count * ctas_per_sm CTAs, `chunk`
+// tiles per queue grab), seam merge inside each cutout, canonical form
+void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchImg *imgs, const BatchTile *tiles,
+                        int ntiles, int chunk, unsigned *next, float *gval, unsigned long long *node, int *parent,
+                        unsigned char *isroot, unsigned long long *num_nodes, unsigned *err, int ctas_per_sm,
+                        int sm_count, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // attribute records (structure of arrays over pixels; valid at level roots)
@@ -85,6 +107,21 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_s
 void launch_attributes_rest(const TreeView &t, AttrBufs &a, unsigned R, unsigned *count, void *scratch, unsigned *err,
                             int sm_count, cudaStream_t s);
 
+// the bottom-up part of launch_attributes alone (after a pixel pass done elsewhere)
+void launch_attributes_up(const TreeView &t, AttrBufs &a, unsigned *count, int up_steps, unsigned *err, int sm_count,
+                          cudaStream_t s);
+// launch_attributes_rest without the host read of the count: scratch sized for
+// `cap` nodes (attr_rest_bytes(group, cap)); a count above cap raises
+// DEVERR_CAPACITY and leaves the records incomplete.  Issues no host
+// synchronisation, so it can be captured in a CUDA graph.
+void launch_attributes_rest_cap(const TreeView &t, AttrBufs &a, unsigned cap, unsigned *count, void *scratch,
+                                unsigned *err, int sm_count, cudaStream_t s);
+int batch_max_ctas_per_sm(int dtype, int tw, int th);
+// per-pixel contributions of a batch, walked tile by tile (coordinates inside the cutout)
+void launch_batch_attr_pixels(const Geom &bg, const BatchImg *imgs, const BatchTile *tiles, int ntiles,
+                              const float *gval, const int *parent, const unsigned char *isroot, AttrBufs &a,
+                              int sm_count, cudaStream_t s);
+
 // attribute readout of every level root into a double array (NaN elsewhere)
 void launch_node_attr(const TreeView &t, const AttrBufs &a, int attr, bool area, double *out, int sm_count,
                       cudaStream_t s);
@@ -109,5 +146,33 @@ void launch_check(const TreeView &t, const AttrBufs &a, int attr, float *out, in
 void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *l1, int n1, int a2,
                      const float *l2, int n2, double *spec, int sm_count, cudaStream_t s);
 void launch_level_out(const TreeView &t, float *out, int sm_count, cudaStream_t s);
+// per-cutout 2-D spectra of a batch, spec[img*n1*n2 + s1 + s2*n1] (accumulated)
+void launch_batch_spectrum(const Geom &bg, const BatchImg *imgs, const BatchTile *tiles, int ntiles, const int *parent,
+                           const unsigned char *isroot, const float *gval, const AttrBufs &a, int a1, const float *l1,
+                           int n1, int a2, const float *l2, int n2, const float *pixdim, double *spec, int sm_count,
+                           cudaStream_t s);
+
+// Adjoint of out = direct-rule filter (v = d loss / d out, per pixel; target =
+// the resolved surviving node of every level root, from launch_filter) and of
+// spec = 2-D pattern spectra (w = d loss / d spec, per cutout), with the tree
+// held fixed: d loss / d level(u) is accumulated in acc (double, per pixel,
+// zeroed by the caller) at the level root u that carries each node's level, then
+// written to grad (float).  `offs` lists the first pixel of each of `count`
+// cutouts (count = 1, offs = {0} for one image).
+struct AdjointArgs {
+    const int *target = nullptr;     // null: no filter term
+    const float *v = nullptr;
+    const double *w = nullptr;       // null: no spectrum term
+    int a1 = 0, n1 = 0, a2 = 0, n2 = 0;
+    const float *l1 = nullptr, *l2 = nullptr;
+    const long long *offs = nullptr;
+    int count = 1;
+    double *acc = nullptr;
+    float *grad = nullptr;
+};
+void launch_adjoint(const TreeView &t, const AttrBufs &a, const AdjointArgs &j, int sm_count, cudaStream_t s);
+// direct rule up to the resolved targets (flag + resolve), no output pass
+void launch_direct_targets(const TreeView &t, const AttrBufs &a, int attr, double lambda, const FilterWork &w,
+                           unsigned *err, int sm_count, cudaStream_t s);
 
 }  // namespace dcf

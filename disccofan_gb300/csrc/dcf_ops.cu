@@ -379,4 +379,75 @@ void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *
     prof_end(P_SPECTRUM, s);
 }
 
+// ---------------------------------------------------------------------------
+// adjoint (no reference counterpart)
+// ---------------------------------------------------------------------------
+// With the tree fixed, the direct-rule output out(p) = level(target(node(p))) and
+// the spectrum term dh(u) * area(u), dh(u) = level(u) - level(parent(u)), are
+// linear in the levels; a node's level is the value of its level root pixel.  So
+//   d loss / d level(s) += v(p)                       for target(node(p)) = s,
+//   d loss / d level(u) += w(bin(u)) * area(u),  d loss / d level(parent(u)) -= same.
+__device__ __forceinline__ int cutout_of(const long long *offs, int count, long long p)
+{
+    int lo = 0, hi = count - 1;  // last cutout whose first pixel is <= p
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (offs[mid] <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_adjoint(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                          AttrBufs a, AdjointArgs j, float pd0, float pd1, float pd2)
+{
+    const float pd[3] = {pd0, pd1, pd2};
+    GRID_LOOP(p, g.N)
+    {
+        const bool root = isroot[p];
+        if (j.target) {
+            const int s = j.target[root ? (int)p : parent[p]];
+            if (s >= 0) atomicAdd(j.acc + s, (double)j.v[p]);
+        }
+        if (!j.w || !root) continue;
+        const double ar = area_value(a, (int)p, pd);
+        const int s1 = find_scale(j.l1, j.n1, j.a1 < 0 ? ar : attr_value(a, j.a1, (int)p, pd));
+        const int s2 = j.n2 <= 1 ? 0 : find_scale(j.l2, j.n2, j.a2 < 0 ? ar : attr_value(a, j.a2, (int)p, pd));
+        const int img = j.count > 1 ? cutout_of(j.offs, j.count, p) : 0;
+        const double c = j.w[(long long)img * j.n1 * j.n2 + s1 + s2 * j.n1] * ar;
+        if (c == 0.0) continue;
+        atomicAdd(j.acc + p, c);
+        const int q = parent[p];
+        if (q != NONE) atomicAdd(j.acc + q, -c);
+    }
+}
+
+__global__ void k_adjoint_out(long long n, const double *__restrict__ acc, float *grad)
+{
+    GRID_LOOP(p, n) grad[p] = (float)acc[p];
+}
+
+void launch_adjoint(const TreeView &t, const AttrBufs &a, const AdjointArgs &j, int sm, cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+    prof_begin(P_ADJOINT, s);
+    k_adjoint<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, a, j, t.pixdim[0], t.pixdim[1], t.pixdim[2]);
+    k_adjoint_out<<<nb, 256, 0, s>>>(t.g.N, j.acc, j.grad);
+    prof_end(P_ADJOINT, s);
+}
+
+// direct rule without the output pass: survive flags and resolved targets
+void launch_direct_targets(const TreeView &t, const AttrBufs &a, int attr, double lambda, const FilterWork &w,
+                           unsigned *err, int sm, cudaStream_t s)
+{
+    const int nb = grid_for(t.g.N, 256, sm);
+    prof_begin(P_FLAG, s);
+    k_flag<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
+                              w.target);
+    prof_end(P_FLAG, s);
+    prof_begin(P_RESOLVE, s);
+    k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err);
+    prof_end(P_RESOLVE, s);
+}
+
 }  // namespace dcf

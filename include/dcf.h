@@ -149,6 +149,69 @@ dcf_status dcf_pattern_spectrum2d(dcf_ctx *ctx, dcf_tree *tree, int attr1, const
 dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, double lambda, int extract,
                                      float *out_device);
 
+/* ---- batches of 2-D cutouts, and the adjoint (no reference counterparts) ---- */
+typedef struct dcf_batch dcf_batch;
+
+/* Operations of a batch run (and of dcf_tree_adjoint).  filter_attr >= 0: the
+ * direct-rule filter (keep nodes whose attribute >= lambda; max-tree, no
+ * extract).  spec_attr1 >= 0: a 2-D pattern spectrum per cutout with the
+ * argument rules of dcf_pattern_spectrum2d (spec_attr2 = 0 bins by area; n2 = 1
+ * with lvec2 = {0} gives a 1-D spectrum).  lvec1/lvec2 are host arrays that
+ * include the leading 0.  use_graph = 1: the device work of a run is recorded as
+ * one CUDA graph (on the second run; the first learns a buffer capacity) and
+ * replayed while the pointers and operations stay the same. */
+typedef struct {
+    int filter_attr;
+    double lambda;
+    int spec_attr1;
+    const float *lvec1;
+    int n1;
+    int spec_attr2;
+    const float *lvec2;
+    int n2;
+    int use_graph;
+} dcf_op_set;
+
+/* A batch of `count` 2-D cutouts of one dtype, widths[i] x heights[i] pixels,
+ * built as max-trees with connectivity 4 or 8 and the attribute group of
+ * attr_idx.  Pixels are concatenated: cutout i starts at element sum_{j<i}
+ * widths[j]*heights[j] (x fastest inside a cutout); at most 2^31-1 in total.
+ * Every device buffer is allocated here (or on the first run needing it).
+ * Destroy batches before their context. */
+dcf_status dcf_batch_create(dcf_ctx *ctx, int count, const uint32_t *widths, const uint32_t *heights, int dtype,
+                            int connectivity, int attr_idx, const float *pixdim, dcf_batch **out);
+dcf_status dcf_batch_destroy(dcf_batch *batch);
+/* schedule[4] = tile width, tile height, CTAs per SM, tiles per queue grab;
+ * graph_kernels = kernel nodes in the recorded graph (0: none recorded) */
+dcf_status dcf_batch_info(const dcf_batch *batch, uint64_t *total_pixels, uint64_t *num_nodes, int *schedule,
+                          uint64_t *graph_kernels);
+/* Persistent tile-build schedule (ctas_per_sm <= 0: as many as fit). */
+dcf_status dcf_batch_set_schedule(dcf_ctx *ctx, dcf_batch *batch, int tile_w, int tile_h, int ctas_per_sm, int chunk);
+/* Time the build phase over tile shapes, then CTAs per SM and queue chunk for the
+ * best shape, on these pixels; keep the fastest schedule.  Leaves no valid trees. */
+dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *batch, const void *pixels, int on_device, int repeats,
+                              double *best_ms);
+/* Build every cutout's tree and attributes, then the requested operations:
+ * filtered (N floats, may be NULL) and spectra (count * n1 * n2 doubles,
+ * spectra[i*n1*n2 + s1 + s2*n1], OVERWRITTEN; may be NULL).  With
+ * outputs_on_device = 0 both are host arrays. */
+dcf_status dcf_batch_run(dcf_ctx *ctx, dcf_batch *batch, const void *pixels, int pixels_on_device,
+                         const dcf_op_set *ops, float *filtered, double *spectra, int outputs_on_device);
+/* Canonical parents of the last run, as indices inside each cutout (-1: root). */
+dcf_status dcf_batch_parent(dcf_ctx *ctx, dcf_batch *batch, int64_t *parent, int on_device);
+/* Attribute of every level root of the last run (NaN elsewhere). */
+dcf_status dcf_batch_node_attribute(dcf_ctx *ctx, dcf_batch *batch, int attr_idx, double *out, int on_device);
+/* Adjoint of the last run's operations with its trees held fixed (float32
+ * pixels): grad_pixels = d loss / d pixels for loss = sum(grad_filtered *
+ * filtered) + sum(grad_spectra * spectra).  Either cotangent may be NULL.  A
+ * node's level is its level root's pixel value, so each node's terms land on
+ * that pixel. */
+dcf_status dcf_batch_adjoint(dcf_ctx *ctx, dcf_batch *batch, const float *grad_filtered, const double *grad_spectra,
+                             float *grad_pixels, int on_device);
+/* The same adjoint for one tree (a float32 max-tree) and the operations in ops. */
+dcf_status dcf_tree_adjoint(dcf_ctx *ctx, dcf_tree *tree, const dcf_op_set *ops, const float *grad_filtered,
+                            const double *grad_spectrum, float *grad_pixels, int on_device);
+
 /* ---- lambda vectors ---- */
 /* Read a "#LambdaVector file..." file: out[0] = 0, out[i] = value_i / imscale.
  * *num_lambdas receives K+1; fails with DCF_ERR_INVALID if capacity < K+1. */

@@ -306,3 +306,69 @@ class Port:
         if self.lib.dco_node_attr(self.t, attr, int(area), out.ctypes.data) != 0:
             raise RuntimeError("node_attr failed")
         return out
+
+
+def find_scale(lvec, values) -> np.ndarray:
+    """The reference's bin search (pattern.c:7-24) over many values: the last bin
+    whose lambda is <= the value (the bisection itself, so NaN lands where it does
+    in C: bin 0)."""
+    lv = np.asarray(lvec, np.float32).astype(np.float64)
+    v = np.asarray(values, np.float64)
+    n = lv.size
+    upper = np.full(v.shape, n - 1, np.int64)
+    lower = np.zeros(v.shape, np.int64)
+    top = v >= lv[n - 1]
+    mid = (upper + lower) // 2
+    active = ~top & (mid != lower)
+    while active.any():
+        ge = v >= lv[mid]
+        lower = np.where(active & ge, mid, lower)
+        upper = np.where(active & ~ge, mid, upper)
+        mid = (upper + lower) // 2
+        active = active & (mid != lower)
+    return np.where(top, n - 1, lower)
+
+
+def adjoint_fp64(parent, gval, v=None, filter_values=None, lam=0.0, w=None, area=None, bin1=None, lvec1=None,
+                 bin2=None, lvec2=None) -> np.ndarray:
+    """FP64 CPU adjoint of sum(v * filtered) + sum(w * spectrum) with the tree fixed.
+
+    parent: canonical parent array (pixel -> level root, level root -> parent's
+    level root, root -> -1), e.g. from the reference's flood.  Filter: the direct
+    rule of filtering.c:102-153 -- a pixel takes the level of its nearest
+    ancestor-or-self node whose attribute (filter_values, per level root) is >=
+    lam, or 0.  Spectrum: pattern.c:110-203 -- every level root u adds
+    (level(u) - level(parent(u))) * area(u) to bin [find_scale(bin2(u)),
+    find_scale(bin1(u))] of w's [n2, n1] layout.  Both are linear in the levels,
+    and a node's level is its level root's pixel value.
+    """
+    par = np.asarray(parent, np.int64)
+    g = np.asarray(gval, np.float64)
+    n = par.size
+    idx = np.arange(n)
+    isroot = (par < 0) | (g[np.maximum(par, 0)] != g)
+    node = np.where(isroot, idx, par)
+    grad = np.zeros(n, np.float64)
+    roots = idx[isroot]
+    if v is not None:
+        keep = np.zeros(n, bool)
+        keep[roots] = np.asarray(filter_values, np.float64)[roots] >= lam
+        target = np.full(n, -1, np.int64)
+        for u in roots[np.argsort(g[roots], kind="stable")]:  # parents before children
+            if keep[u]:
+                target[u] = u
+            elif par[u] >= 0:
+                target[u] = target[par[u]]
+        t = target[node]
+        ok = t >= 0
+        np.add.at(grad, t[ok], np.asarray(v, np.float64).ravel()[ok])
+    if w is not None:
+        w2 = np.asarray(w, np.float64)
+        s1 = find_scale(lvec1, np.asarray(bin1, np.float64)[roots])
+        s2 = find_scale(lvec2, np.asarray(bin2, np.float64)[roots]) if w2.shape[0] > 1 else np.zeros_like(s1)
+        c = w2[s2, s1] * np.asarray(area, np.float64)[roots]
+        np.add.at(grad, roots, c)
+        pr = par[roots]
+        has = pr >= 0
+        np.add.at(grad, pr[has], -c[has])
+    return grad
