@@ -38,8 +38,16 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "Mpx/s tree build+filter+spectrum (max+min tree), 1 GB300"
+METRIC = "Mpx/s tree build+filter+spectrum (% HBM roofline); fwd+adjoint/fwd time, 1 GB300"
 WORKLOAD = "16384^2 u16 log-normal + 1e5 sources; max+min tree, 8-conn, area opening 1000, 2D spectrum bbox-elong x area 21x21"
+
+
+_T0 = time.perf_counter()
+
+
+def log(msg: str):
+    """Progress on stderr (the JSON result is the only line on stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:8.1f}s] {msg}", file=sys.stderr, flush=True)
 
 
 def env_rank():
@@ -306,7 +314,238 @@ def run_ours(args):
     }
     if not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(img, args.cpu_sample, reps=1)
+    del img, d_out, d_spec, h_img
+    log(f"main workload: {ms:.1f} ms/step")
+    if not args.no_batch:
+        result["batch"] = run_batch(args, ctx, stream)
+    if not args.no_adjoint:
+        result["adjoint"] = run_adjoint(args, ctx, stream)
     return result
+
+
+# ---------------------------------------------------------------------------
+# batched cutouts: one recorded CUDA graph per step vs a loop of the plain API
+# ---------------------------------------------------------------------------
+def make_cutouts(count: int = 4096, seed: int = 4, device="cuda"):
+    """count float32 cutouts, width and height independently log-uniform in [64, 1024]:
+    unit Gaussian noise blurred with sigma = 2 px plus 1..50 Gaussian sources (sigma
+    U(1, 5) px, peak U(3, 10) x the background's std).  Backgrounds are windows of
+    one large blurred field.  Returns (shapes [(h, w)], concatenated pixels on device)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    ws = np.rint(np.exp(rng.uniform(np.log(64), np.log(1024), count))).astype(np.int64)
+    hs = np.rint(np.exp(rng.uniform(np.log(64), np.log(1024), count))).astype(np.int64)
+    F = 8192
+    noise = torch.from_numpy(rng.standard_normal((F, F), dtype=np.float32)).to(device)
+    fy = torch.fft.fftfreq(F, device=device)
+    fx = torch.fft.rfftfreq(F, device=device)
+    g = torch.exp(-2.0 * (np.pi ** 2) * 4.0 * (fy[:, None] ** 2 + fx[None, :] ** 2))
+    field = torch.fft.irfft2(torch.fft.rfft2(noise) * g, s=(F, F))
+    del noise
+    std = float(field.std())
+    sizes = hs * ws
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    pix = torch.empty(int(sizes.sum()), dtype=torch.float32, device=device)
+    oy = rng.integers(0, F - hs + 1)
+    ox = rng.integers(0, F - ws + 1)
+    for i in range(count):
+        pix[offs[i]:offs[i] + sizes[i]] = field[oy[i]:oy[i] + hs[i], ox[i]:ox[i] + ws[i]].reshape(-1)
+    # sources, all cutouts at once (in chunks)
+    k = rng.integers(1, 51, count)
+    img = np.repeat(np.arange(count), k)
+    cy = rng.uniform(0, hs[img])
+    cx = rng.uniform(0, ws[img])
+    sg = rng.uniform(1, 5, img.size)
+    pk = rng.uniform(3, 10, img.size) * std
+    r = 12
+
+    def t(a, dt=torch.float64):
+        return torch.from_numpy(np.asarray(a)).to(device=device, dtype=dt)
+
+    off = torch.arange(-r, r + 1, device=device, dtype=torch.float64)
+    for lo in range(0, img.size, 20000):
+        sl = slice(lo, lo + 20000)
+        tcx, tcy, tsg, tpk = t(cx[sl]), t(cy[sl]), t(sg[sl]), t(pk[sl])
+        th, tw, to = t(hs[img[sl]], torch.int64), t(ws[img[sl]], torch.int64), t(offs[img[sl]], torch.int64)
+        px = torch.floor(tcx)[:, None, None] + off[None, None, :]
+        py = torch.floor(tcy)[:, None, None] + off[None, :, None]
+        d2 = (px - tcx[:, None, None]) ** 2 + (py - tcy[:, None, None]) ** 2
+        val = (tpk[:, None, None] * torch.exp(-d2 / (2 * tsg[:, None, None] ** 2))).float()
+        ix, iy = px.expand_as(val).long(), py.expand_as(val).long()
+        ok = (ix >= 0) & (ix < tw[:, None, None]) & (iy >= 0) & (iy < th[:, None, None])
+        flat = (to[:, None, None] + iy * tw[:, None, None] + ix)[ok]
+        pix.index_put_((flat,), val[ok], accumulate=True)
+    return [(int(h), int(w)) for h, w in zip(hs, ws)], pix
+
+
+def run_batch(args, ctx, stream):
+    """The batched workload: 4096 float32 cutouts (64..1024 a side), max-tree 8-conn,
+    inertia group, 2-D spectrum inertia trace (13) x area (0) on 24 log thresholds each
+    (25 x 25 bins) per cutout."""
+    import torch
+    import disccofan_gb300 as dcf
+    log("batch: generating cutouts")
+    shapes, pix = make_cutouts(args.batch_count)
+    npx = pix.numel()
+    log(f"batch: {len(shapes)} cutouts, {npx} pixels; autotuning")
+    l_tr = dcf.lvec_from_values(np.geomspace(1, 1e11, 24))
+    l_ar = dcf.lvec_from_values(np.geomspace(1, 1 << 20, 24))
+    spec = (13, l_tr, 0, l_ar)
+    b = ctx.batch(shapes, np.float32, connectivity=8, attribute=13)
+    spectra = torch.empty((len(shapes), l_ar.size, l_tr.size), dtype=torch.float64, device="cuda")
+    t0 = time.perf_counter()
+    tune_ms = b.autotune(pix, repeats=1) if not args.no_autotune else None
+    tune_s = time.perf_counter() - t0
+    log(f"batch: autotuned in {tune_s:.1f}s -> {b.info()}")
+    for _ in range(max(args.warmup, 2)):  # learns the capacity, then records the graph
+        b.run(pix, spectrum=spec, use_graph=True, spectra=spectra)
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    launches0 = ctx.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        b.run(pix, spectrum=spec, use_graph=True, spectra=spectra)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = ev0.elapsed_time(ev1) / steps
+    graph_launches = (ctx.launches - launches0) // steps
+    info = b.info()
+    log(f"batch: graph {graph_ms:.1f} ms/step; looping the single-image API")
+    loop_spec = torch.zeros_like(spectra)
+    views = []
+    o = 0
+    for h, w in shapes:
+        views.append(pix[o:o + h * w].view(h, w))
+        o += h * w
+    # the loop is timed on a bounded sample (the first loop_n cutouts) and scaled by
+    # pixels, so that this arm stays within seconds
+    loop_n = min(len(views), args.loop_sample)
+
+    def loop_over(idx):
+        for i in idx:
+            t = ctx.build(views[i], connectivity=8, tree_type="max", attribute=13)
+            t.pattern_spectrum2d(13, l_tr, 0, l_ar, out=loop_spec[i])
+            t.close()
+
+    loop_over(range(min(16, loop_n)))  # warm-up
+    loop_spec.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop_over(range(loop_n))
+    torch.cuda.synchronize()
+    loop_px = sum(h * w for h, w in shapes[:loop_n])
+    loop_ms = (time.perf_counter() - t0) * 1e3 * npx / loop_px
+    log(f"batch: loop {loop_ms:.1f} ms/step (scaled from {loop_n} cutouts)")
+    ref = loop_spec[:loop_n]
+    diff = float(((spectra[:loop_n] - ref).abs().max() / ref.abs().max().clamp_min(1e-300)).item())
+    b.close()
+    return {"workload": f"{len(shapes)} f32 cutouts, sides log-uniform 64..1024; max-tree 8-conn, inertia group, "
+                        "2D spectrum inertia-trace x area 25x25 per cutout",
+            "cutouts": len(shapes), "pixels": npx, "nodes": info["nodes"],
+            "graph_ms_per_step": round(graph_ms, 3), "graph_mpx_s": round(npx / 1e6 / (graph_ms * 1e-3), 2),
+            "loop_ms_per_step": round(loop_ms, 3), "loop_mpx_s": round(npx / 1e6 / (loop_ms * 1e-3), 2),
+            "speedup_vs_loop": round(loop_ms / graph_ms, 2), "max_rel_spectrum_diff_vs_loop": diff,
+            "loop_sample": f"first {loop_n} cutouts ({loop_px} px), one pass, scaled to the batch's pixels",
+            "schedule": {"tile": info["tile"], "ctas_per_sm": info["ctas_per_sm"], "chunk": info["chunk"]},
+            "autotune": {"best_build_ms": None if tune_ms is None else round(tune_ms, 3), "seconds": round(tune_s, 2)},
+            "graph_kernels": info["graph_kernels"], "gpu_launches_per_step": int(graph_launches), "steps": steps}
+
+
+# ---------------------------------------------------------------------------
+# differentiable workload: forward vs forward + adjoint (tree recomputed)
+# ---------------------------------------------------------------------------
+def distinct_values(im):
+    """Separate exact ties of a float32 image while keeping its order: after a stable
+    sort, every value not above its predecessor moves up to the next float (repeated
+    until all are distinct; a 512^2 image of continuous values has a few hundred
+    float32 ties and the loop ends after a few passes)."""
+    import torch
+    flat = im.reshape(-1)
+    vals, idx = torch.sort(flat, stable=True)
+    for _ in range(64):
+        dup = vals[1:] <= vals[:-1]
+        if not bool(dup.any()):
+            break
+        nxt = torch.nextafter(vals[:-1], torch.full_like(vals[:-1], float("inf")))
+        vals[1:] = torch.where(dup, nxt, vals[1:])
+    else:
+        raise RuntimeError("could not separate tied values")
+    out = torch.empty_like(flat)
+    out[idx] = vals
+    return out.view_as(im)
+
+
+def make_distinct_images(count: int = 256, size: int = 512, seed: int = 5, device="cuda"):
+    """count x size^2 float32: Gaussian blur (sigma 2) of N(0,1) plus 0.05 N(0,1) i.i.d.,
+    with every image's values distinct (distinct_values)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    fy = torch.fft.fftfreq(size, device=device)
+    fx = torch.fft.rfftfreq(size, device=device)
+    g = torch.exp(-2.0 * (np.pi ** 2) * 4.0 * (fy[:, None] ** 2 + fx[None, :] ** 2))
+    out = torch.empty((count, size, size), dtype=torch.float32, device=device)
+    for i in range(count):
+        a = torch.from_numpy(rng.standard_normal((size, size), dtype=np.float32)).to(device)
+        e = torch.from_numpy(rng.standard_normal((size, size), dtype=np.float32)).to(device)
+        im = distinct_values((torch.fft.irfft2(torch.fft.rfft2(a) * g, s=(size, size)) + 0.05 * e).float())
+        assert torch.unique(im).numel() == im.numel()
+        out[i] = im
+    return out
+
+
+def run_adjoint(args, ctx, stream):
+    """256 float32 512^2 images: area opening (lambda 64, direct rule) and the 2-D
+    spectrum elongation (14) x area (0) on 16 log thresholds each, then the adjoint of
+    sum(w * spectra) + sum(v * filtered), w, v ~ N(0, 1), through the autograd Function
+    (backward rebuilds the trees)."""
+    import torch
+    import disccofan_gb300 as dcf
+    from disccofan_gb300.autograd import filter_and_spectrum
+    count, size = args.adj_count, 512
+    log("adjoint: generating images")
+    x = make_distinct_images(count, size)
+    log("adjoint: timing")
+    l_el = dcf.lvec_from_values(np.geomspace(1, 100, 16))
+    l_ar = dcf.lvec_from_values(np.geomspace(1, size * size, 16))
+    spec = (14, l_el, 0, l_ar)
+    b = ctx.batch([(size, size)] * count, np.float32, connectivity=8, attribute=14)
+    rng = np.random.default_rng(6)
+    v = torch.from_numpy(rng.standard_normal((count, size, size), dtype=np.float32)).to("cuda")
+    w = torch.from_numpy(rng.standard_normal((count, l_ar.size, l_el.size))).to("cuda")
+    xg = x.clone().requires_grad_(True)
+
+    def fwd():
+        with torch.no_grad():
+            return filter_and_spectrum(b, x, 0, 64.0, spec)
+
+    def fwd_adj():
+        xg.grad = None
+        f, s = filter_and_spectrum(b, xg, 0, 64.0, spec)
+        ((v * f).sum(dtype=torch.float64) + (w * s).sum()).backward()
+        return xg.grad
+
+    def timed(fn, n):
+        for _ in range(max(args.warmup, 2)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    n = max(1, args.steps)
+    t_fwd = timed(fwd, n)
+    t_both = timed(fwd_adj, n)
+    t_f = min(t_fwd, timed(fwd, n))
+    b.close()
+    return {"workload": f"{count} f32 {size}^2 images (distinct values); area opening 64 + 2D spectrum "
+                        "elongation x area 17x17; adjoint of sum(w*spectra)+sum(v*filtered), tree recomputed",
+            "fwd_ms": round(t_f, 3), "fwd_adjoint_ms": round(t_both, 3), "ratio": round(t_both / t_f, 3),
+            "target_ratio": 2.5, "fwd_mpx_s": round(count * size * size / 1e6 / (t_f * 1e-3), 2), "steps": n}
 
 
 # ---------------------------------------------------------------------------
@@ -372,6 +611,12 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-cutout workload")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint workload")
+    ap.add_argument("--no-autotune", action="store_true", help="batched workload: keep the default schedule")
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--loop-sample", type=int, default=512, help="cutouts timed through the single-image API")
+    ap.add_argument("--adj-count", type=int, default=256)
     args = ap.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
     if res is not None:

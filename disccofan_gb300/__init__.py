@@ -115,6 +115,7 @@ def library() -> C.CDLL:
         "dcf_batch_destroy": [vp],
         "dcf_batch_info": [vp, C.POINTER(u64), C.POINTER(u64), vp, C.POINTER(u64)],
         "dcf_batch_set_schedule": [vp, vp, i, i, i, i],
+        "dcf_batch_set_merge": [vp, vp, i, i],
         "dcf_batch_autotune": [vp, vp, vp, i, i, C.POINTER(d)],
         "dcf_batch_run": [vp, vp, vp, i, C.POINTER(OpSet), vp, vp, i],
         "dcf_batch_parent": [vp, vp, vp, i],
@@ -449,14 +450,17 @@ class Batch:
 
     def info(self):
         n, m, g = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        sch = (C.c_int * 4)()
+        sch = (C.c_int * 6)()
         self.ctx.check(self.ctx.lib.dcf_batch_info(self.h, C.byref(n), C.byref(m), sch, C.byref(g)), "batch_info")
         return {"pixels": n.value, "nodes": m.value, "tile": (sch[0], sch[1]), "ctas_per_sm": sch[2],
-                "chunk": sch[3], "graph_kernels": g.value}
+                "chunk": sch[3], "seam_buckets": sch[4], "up_steps": sch[5], "graph_kernels": g.value}
 
     def set_schedule(self, tile=(64, 64), ctas_per_sm=0, chunk=1):
         self.ctx.check(self.ctx.lib.dcf_batch_set_schedule(self.ctx.h, self.h, tile[0], tile[1], ctas_per_sm, chunk),
                        "set_schedule")
+
+    def set_merge(self, seam_buckets: int = 16, up_steps: int = 2048):
+        self.ctx.check(self.ctx.lib.dcf_batch_set_merge(self.ctx.h, self.h, seam_buckets, up_steps), "set_merge")
 
     def autotune(self, pixels, repeats: int = 3) -> float:
         p, dev = self._pixels(pixels)

@@ -42,9 +42,10 @@ struct dcf_ctx {
     int tile2d[2] = {64, 64};         // build tile of 2-D images (width, height)
     int tile3d[3] = {16, 16, 16};     // build tile of 3-D images
     int level_sync = 1;               // barrier between band-merge levels inside a tile
+    int seam_buckets = 0;             // level buckets of the seam merge (0: every seam edge at once)
     std::mutex trees_mu;
     std::set<dcf_tree *> trees;       // live trees; orphaned (stream cleared) when the context goes
-    DevBuf scratch[12];               // reusable work buffers (filter, spectra, attributes)
+    DevBuf scratch[16];               // reusable work buffers (filter, spectra, attributes, seams)
     bool prof_on = false;
     ProfEvent *prof_ev = nullptr;     // recorded events, in launch order
     int prof_n = 0, prof_cap = 0;
@@ -240,6 +241,10 @@ dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out)
         }
     }
     if (const char *e = getenv("DCF_LEVEL_SYNC")) ctx->level_sync = atoi(e) != 0;
+    if (const char *e = getenv("DCF_SEAM_BUCKETS")) {
+        int v = atoi(e);
+        if (v >= 0 && v <= 1024) ctx->seam_buckets = v;
+    }
     if (const char *e = getenv("DCF_UP_STEPS")) {
         int v = atoi(e);
         if (v >= 0 && v < (1 << 20)) ctx->up_steps = v;
@@ -534,6 +539,15 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
         ba.num_nodes = t->num_nodes;
         ba.err = ctx->d_err;
         ba.sm_count = ctx->sm_count;
+        if (ctx->seam_buckets > 0) {
+            const long long ntiles = (long long)((W + t->g.tw - 1) / t->g.tw) * ((H + t->g.th - 1) / t->g.th) *
+                                     ((D + t->g.td - 1) / t->g.td);
+            const long long cap = seam_edge_bound(t->g, ntiles);
+            void *sm;
+            st = scratch(ctx, 12, seam_edges_bytes(cap, ctx->seam_buckets), &sm);
+            if (st != DCF_OK) goto fail;
+            ba.seam = seam_edges_carve(sm, cap, ctx->seam_buckets);
+        }
         launch_build(ba, ctx->stream);
         st = check_launch(ctx, 4);
         if (st != DCF_OK) goto fail;
@@ -944,6 +958,8 @@ struct dcf_batch {
     long long *d_offs = nullptr;
     // schedule: tile shape, CTAs per SM of the persistent kernel, tiles per queue grab
     int tw = 64, th = 64, ctas = 1, chunk = 1;
+    int seam_buckets = 16;                   // level buckets of the seam merge (0: all edges at once)
+    int up_steps = 2048;                     // bottom-up fold steps per walker
     int ntiles = 0;
     size_t tiles_cap = 0;
     BatchTile *d_tiles = nullptr;
@@ -956,6 +972,9 @@ struct dcf_batch {
     unsigned char *isroot = nullptr;
     void *attr_mem = nullptr;
     AttrBufs attr;
+    void *seam_mem = nullptr;                // level-ordered seam merge scratch
+    size_t seam_bytes = 0;
+    SeamEdges seam;
     unsigned rest_cap = 0;                   // graph runs: pointer-jumping capacity (0: not learned yet)
     size_t rest_bytes = 0;
     void *rest_mem = nullptr;
@@ -1019,6 +1038,8 @@ static TreeView batch_view(const dcf_batch *b)
     return v;
 }
 
+static constexpr int SEAM_BUCKETS_MAX = 256;
+
 static dcf_status batch_set_tiles(dcf_ctx *ctx, dcf_batch *b, int tw, int th, int ctas, int chunk)
 {
     if (tw < 1 || th < 1 || tw * th > TILE_MAX_PIX)
@@ -1040,6 +1061,25 @@ static dcf_status batch_set_tiles(dcf_ctx *ctx, dcf_batch *b, int tw, int th, in
     }
     CU(cudaMemcpyAsync(b->d_tiles, tl.data(), tl.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
+    {
+        Geom tg{};
+        tg.conn = b->conn;
+        tg.tw = tw;
+        tg.th = th;
+        const long long cap = batch_seam_edge_bound(tg, b->imgs.data(), b->count);
+        const size_t need = seam_edges_bytes(cap, SEAM_BUCKETS_MAX);
+        if (need > b->seam_bytes) {
+            batch_drop_graph(b);
+            if (b->seam_mem) CU(cudaFree(b->seam_mem));
+            b->seam_mem = nullptr;
+            b->seam_bytes = 0;
+            CU(cudaMalloc(&b->seam_mem, need));
+            b->seam_bytes = need;
+        }
+        // laid out for the largest bucket count, so set_merge can change it in place
+        b->seam = seam_edges_carve(b->seam_mem, cap, SEAM_BUCKETS_MAX);
+        b->seam.buckets = b->seam_buckets;
+    }
     b->ntiles = (int)tl.size();
     b->tw = tw;
     b->th = th;
@@ -1077,11 +1117,11 @@ static dcf_status batch_forward(dcf_ctx *ctx, dcf_batch *b, const void *px, floa
     CU(cudaMemsetAsync(b->d_nodes, 0, sizeof(unsigned long long), s));
     launch_stats(b->dtype, px, b->N, b->d_misc + 2, b->d_misc + 3, b->d_misc + 4, sm, s);
     launch_batch_build(b->dtype, px, v.g, b->d_imgs, b->d_tiles, b->ntiles, b->chunk, b->d_misc, b->gval, b->node,
-                       b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, sm, s);
+                       b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, b->seam, sm, s);
     CU(attr_zero(b->attr, (size_t)b->N, b->attr_mem, sm, s));
     launch_batch_attr_pixels(v.g, b->d_imgs, b->d_tiles, b->ntiles, b->gval, b->parent, b->isroot, b->attr, sm, s);
     unsigned *count = b->d_misc + 1;
-    launch_attributes_up(v, b->attr, count, ctx->up_steps, ctx->d_err, sm, s);
+    launch_attributes_up(v, b->attr, count, b->up_steps, ctx->d_err, sm, s);
     if (graph) {
         launch_attributes_rest_cap(v, b->attr, b->rest_cap, count, b->rest_mem, ctx->d_err, sm, s);
     } else {
@@ -1173,6 +1213,7 @@ dcf_status dcf_batch_create(dcf_ctx *ctx, int count, const uint32_t *widths, con
     b->conn = connectivity;
     b->attr_idx = attr_idx;
     b->group = ATTR_GROUP[attr_idx];
+    b->up_steps = ctx->up_steps;
     if (pixdim)
         for (int i = 0; i < 3; i++) b->pixdim[i] = pixdim[i];
     std::vector<long long> offs(count);
@@ -1233,7 +1274,7 @@ dcf_status dcf_batch_destroy(dcf_batch *b)
     batch_drop_graph(b);
     void *bufs[] = {b->d_imgs, b->d_offs, b->d_tiles, b->d_misc, b->pixels, b->gval, b->node, b->parent, b->isroot,
                     b->attr_mem, b->rest_mem, b->flag, b->target, b->filtered, b->spectra, b->lvec, b->adj_acc,
-                    b->adj_io, b->adj_w};
+                    b->adj_io, b->adj_w, b->seam_mem};
     for (void *p : bufs)
         if (p) cudaFree(p);
     delete b;
@@ -1258,6 +1299,8 @@ dcf_status dcf_batch_info(const dcf_batch *b, uint64_t *total_pixels, uint64_t *
         schedule[1] = b->th;
         schedule[2] = b->ctas;
         schedule[3] = b->chunk;
+        schedule[4] = b->seam_buckets;
+        schedule[5] = b->up_steps;
     }
     if (graph_kernels) *graph_kernels = b->graph_kernels;
     return DCF_OK;
@@ -1268,6 +1311,22 @@ dcf_status dcf_batch_set_schedule(dcf_ctx *ctx, dcf_batch *b, int tile_w, int ti
     ActiveScope active_scope_(ctx);
     if (!ctx || !b) return DCF_ERR_INVALID;
     return batch_set_tiles(ctx, b, tile_w, tile_h, ctas_per_sm, chunk);
+}
+
+dcf_status dcf_batch_set_merge(dcf_ctx *ctx, dcf_batch *b, int seam_buckets, int up_steps)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !b) return DCF_ERR_INVALID;
+    if (seam_buckets < 0 || seam_buckets > SEAM_BUCKETS_MAX)
+        return set_err(ctx, DCF_ERR_INVALID, "seam buckets %d (0..%d)", seam_buckets, SEAM_BUCKETS_MAX);
+    if (up_steps < 0 || up_steps >= (1 << 24)) return set_err(ctx, DCF_ERR_INVALID, "up_steps %d", up_steps);
+    batch_drop_graph(b);
+    b->seam_buckets = seam_buckets;
+    b->seam.buckets = seam_buckets;
+    b->up_steps = up_steps;
+    b->rest_cap = 0;  // the pointer-jumping capacity is learned again
+    b->valid = false;
+    return DCF_OK;
 }
 
 dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *b, const void *pixels, int on_device, int repeats,
@@ -1294,8 +1353,8 @@ dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *b, const void *pixels, in
         for (int r = 0; r <= repeats; r++) {  // the first pass warms up
             cudaEventRecord(e0, ctx->stream);
             launch_batch_build(b->dtype, px, v.g, b->d_imgs, b->d_tiles, b->ntiles, b->chunk, b->d_misc, b->gval,
-                               b->node, b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, ctx->sm_count,
-                               ctx->stream);
+                               b->node, b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, b->seam,
+                               ctx->sm_count, ctx->stream);
             cudaEventRecord(e1, ctx->stream);
             dcf_status st = check_launch(ctx, 4);
             if (st != DCF_OK) return st;
@@ -1311,7 +1370,7 @@ dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *b, const void *pixels, in
     struct Cand {
         int tw, th, ctas, chunk;
     };
-    static const int shapes[][2] = {{64, 64}, {128, 32}, {32, 128}, {64, 32}, {32, 64}, {32, 32}, {128, 16}, {16, 64}};
+    static const int shapes[][2] = {{64, 64}, {128, 32}, {64, 32}, {32, 32}};
     Cand best{64, 64, 0, 1};
     double best_t = 1e30;
     dcf_status st = DCF_OK;
@@ -1327,7 +1386,7 @@ dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *b, const void *pixels, in
     }
     if (st == DCF_OK) {
         const int maxc = batch_max_ctas_per_sm(b->dtype, best.tw, best.th);
-        for (int c : {1, 2, 4, 8})
+        for (int c : {1, 2, maxc})
             for (int ch : {1, 4}) {
                 if (c > maxc || (c == best.ctas && ch == 1)) continue;
                 double ms;
@@ -1339,12 +1398,54 @@ dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *b, const void *pixels, in
                 }
             }
     }
+    // 3) seam buckets on the build, 4) bottom-up steps on build + attributes
+    int best_buckets = b->seam_buckets, best_up = b->up_steps;
+    if (st == DCF_OK) st = batch_set_tiles(ctx, b, best.tw, best.th, best.ctas, best.chunk);
+    if (st == DCF_OK) {
+        for (int nb : {0, 16, 64}) {
+            if (nb == best_buckets) continue;
+            double ms;
+            b->seam_buckets = b->seam.buckets = nb;
+            if ((st = time_build(&ms)) != DCF_OK) break;
+            if (ms < best_t) {
+                best_t = ms;
+                best_buckets = nb;
+            }
+        }
+        b->seam_buckets = b->seam.buckets = best_buckets;
+    }
+    double best_fwd = 1e30;
+    if (st == DCF_OK) {
+        const dcf_op_set keep = b->ops;
+        b->ops = dcf_op_set{-1, 0.0, -1, nullptr, 0, 0, nullptr, 0, 0};
+        for (int up : {2048, 16384, 131072}) {
+            b->up_steps = up;
+            std::vector<float> t;
+            for (int r = 0; r <= repeats && st == DCF_OK; r++) {
+                cudaEventRecord(e0, ctx->stream);
+                st = batch_forward(ctx, b, px, nullptr, nullptr, false);
+                cudaEventRecord(e1, ctx->stream);
+                if (st == DCF_OK) st = batch_check(ctx, b, nullptr);
+                float x = 0.f;
+                cudaEventElapsedTime(&x, e0, e1);
+                if (r) t.push_back(x);
+            }
+            if (st != DCF_OK) break;
+            std::sort(t.begin(), t.end());
+            if (t[t.size() / 2] < best_fwd) {
+                best_fwd = t[t.size() / 2];
+                best_up = up;
+            }
+        }
+        b->up_steps = best_up;
+        b->ops = keep;
+        b->rest_cap = 0;
+    }
     ctx->prof_on = prof;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != DCF_OK) return st;
-    if ((st = batch_set_tiles(ctx, b, best.tw, best.th, best.ctas, best.chunk)) != DCF_OK) return st;
-    b->valid = false;  // the timed builds left no attributes
+    b->valid = false;  // the timed runs leave no usable state
     if (best_ms) *best_ms = best_t;
     return batch_check(ctx, b, nullptr);
 }

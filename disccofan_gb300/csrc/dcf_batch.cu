@@ -11,7 +11,8 @@
 //
 //   k_batch_tile_build   persistent: grid = SMs x CTAs-per-SM; each CTA takes the
 //                        next tiles from an atomic work counter until none is left.
-//   k_batch_seam         tile-boundary edges inside each cutout.
+//   k_batch_seam(_collect)  tile-boundary edges inside each cutout, merged at once
+//                        or collected for the level-ordered merge.
 //   k_batch_attr_pixels  per-pixel attribute contributions, walked tile by tile so
 //                        each pixel's cutout (and in-cutout coordinates) is known.
 //   k_batch_spectrum     per-cutout 2-D pattern spectra, one shared-memory
@@ -36,7 +37,7 @@ static __device__ __forceinline__ Geom cut_geom(const BatchImg &im, const Geom &
 // the atomic counter *next until the list is exhausted.  Every grab advances the
 // counter, so the loop ends after at most ntiles / chunk + 1 grabs per CTA.
 template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS)
+__global__ void __launch_bounds__(TILE_THREADS, 5)
 k_batch_tile_build(const T *__restrict__ img, Geom bg, const BatchImg *__restrict__ imgs,
                    const BatchTile *__restrict__ tiles, int ntiles, int chunk, unsigned *next,
                    float *__restrict__ gval, unsigned long long *__restrict__ gnode, unsigned *err)
@@ -58,42 +59,79 @@ k_batch_tile_build(const T *__restrict__ img, Geom bg, const BatchImg *__restric
     }
 }
 
-// Seam merge: work item = (tile, face, run of 4 face pixels) over the tile's +x,
-// -x (8-connectivity) and +y faces; 2-D forward offsets never point to -y, so
-// every edge between two tiles of one cutout leaves its low endpoint's tile
-// through one of these faces.  Edges leaving the cutout are skipped.
+// Seam edges of a batch: work item = (tile, face, face pixel, forward offset) over
+// the tile's +x, -x and +y faces; face f takes the offsets pointing out through
+// it.  2-D forward offsets never point to -y, so every edge between two tiles of
+// one cutout leaves its low endpoint's tile through one of these faces.  Edges
+// leaving the cutout are skipped.  One connect per edge and thread.
+__device__ __forceinline__ bool batch_seam_item(const Geom &bg, const BatchImg *imgs, const BatchTile *tiles,
+                                                const Offs &offs, int fmax, long long w, int &p, int &q)
+{
+    const int e = (int)(w % offs.n);
+    long long r = w / offs.n;
+    const int k = (int)(r % fmax);
+    r /= fmax;
+    const int f = (int)(r % 3);
+    const int t = (int)(r / 3);
+    const int dx = offs.d[e][0], dy = offs.d[e][1];
+    if (!(f == 0 ? dx > 0 : f == 1 ? dx < 0 : dy > 0)) return false;
+    const BatchTile tl = tiles[t];
+    const BatchImg im = imgs[tl.img];
+    const int wl = min(bg.tw, im.W - tl.x0), hl = min(bg.th, im.H - tl.y0);
+    if (k >= (f <= 1 ? hl : wl)) return false;
+    const int x = tl.x0 + (f == 0 ? wl - 1 : (f == 1 ? 0 : k));
+    const int y = tl.y0 + (f <= 1 ? k : hl - 1);
+    const int qx = x + dx, qy = y + dy;
+    if (qx < 0 || qx >= im.W || qy >= im.H) return false;
+    p = (int)(im.off + (long long)y * im.W + x);
+    q = (int)(im.off + (long long)qy * im.W + qx);
+    return true;
+}
+
 __global__ void k_batch_seam(unsigned long long *gnode, Geom bg, const BatchImg *__restrict__ imgs,
                              const BatchTile *__restrict__ tiles, int ntiles, unsigned *err)
 {
     GlobalAcc acc{gnode, err, bg.N};
     const Offs offs = forward_offsets(bg.conn);
-    const int TW = bg.tw, TH = bg.th, RUN = 4;
-    const int fmax = TW > TH ? TW : TH;
-    const int nruns = (fmax + RUN - 1) / RUN;
-    const long long work = (long long)ntiles * 3 * nruns;
+    const int fmax = bg.tw > bg.th ? bg.tw : bg.th;
+    const long long work = (long long)ntiles * 3 * fmax * offs.n;
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
          w += (long long)gridDim.x * blockDim.x) {
-        const int run = (int)(w % nruns);
-        const int f = (int)((w / nruns) % 3);
-        const int t = (int)(w / (3LL * nruns));
-        if (f == 1 && bg.conn != 8) continue;
-        const BatchTile tl = tiles[t];
-        const BatchImg im = imgs[tl.img];
-        const int wl = min(TW, im.W - tl.x0), hl = min(TH, im.H - tl.y0);
-        const int flen = f <= 1 ? hl : wl;
-        for (int k = run * RUN; k < min(flen, (run + 1) * RUN); k++) {
-            const int lx = f == 0 ? wl - 1 : (f == 1 ? 0 : k);
-            const int ly = f <= 1 ? k : hl - 1;
-            const int x = tl.x0 + lx, y = tl.y0 + ly;
-            const int p = (int)(im.off + (long long)y * im.W + x);
-            for (int e = 0; e < offs.n; e++) {
-                const int qx = x + offs.d[e][0], qy = y + offs.d[e][1];
-                if (qx < 0 || qx >= im.W || qy >= im.H) continue;
-                if (qx >= tl.x0 && qx < tl.x0 + TW && qy < tl.y0 + TH) continue;
-                connect(acc, p, (int)(im.off + (long long)qy * im.W + qx), MERGE_BOUND_GLOBAL);
-            }
-        }
+        int p, q;
+        if (batch_seam_item(bg, imgs, tiles, offs, fmax, w, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
     }
+}
+
+__global__ void k_batch_seam_collect(const unsigned long long *gnode, Geom bg, const BatchImg *__restrict__ imgs,
+                                     const BatchTile *__restrict__ tiles, int ntiles, SeamEdges e)
+{
+    const Offs offs = forward_offsets(bg.conn);
+    const int fmax = bg.tw > bg.th ? bg.tw : bg.th;
+    const long long work = (long long)ntiles * 3 * fmax * offs.n;
+    const int lane = threadIdx.x & 31;
+    for (long long base = blockIdx.x * (long long)blockDim.x + threadIdx.x - lane; base < work;
+         base += (long long)gridDim.x * blockDim.x) {
+        int p = 0, q = 0;
+        const bool valid = base + lane < work && batch_seam_item(bg, imgs, tiles, offs, fmax, base + lane, p, q);
+        seam_append(e, gnode, valid, p, q);
+    }
+}
+
+long long batch_seam_edge_bound(const Geom &bg, const BatchImg *imgs, int count)
+{
+    const Offs o = forward_offsets(bg.conn);
+    int npx = 0, nmx = 0, npy = 0;
+    for (int i = 0; i < o.n; i++) {
+        npx += o.d[i][0] > 0;
+        nmx += o.d[i][0] < 0;
+        npy += o.d[i][1] > 0;
+    }
+    long long b = 0;
+    for (int i = 0; i < count; i++) {
+        const long long ntx = (imgs[i].W + bg.tw - 1) / bg.tw, nty = (imgs[i].H + bg.th - 1) / bg.th;
+        b += ntx * nty * ((long long)bg.th * (npx + nmx) + (long long)bg.tw * npy);
+    }
+    return b;
 }
 
 // Per-pixel contributions, tile by tile (x, y are coordinates inside the cutout,
@@ -236,7 +274,7 @@ __global__ void k_batch_spectrum(Geom bg, const BatchImg *__restrict__ imgs, con
 void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchImg *imgs, const BatchTile *tiles,
                         int ntiles, int chunk, unsigned *next, float *gval, unsigned long long *node, int *parent,
                         unsigned char *isroot, unsigned long long *num_nodes, unsigned *err, int ctas_per_sm,
-                        int sm, cudaStream_t s)
+                        SeamEdges &seam, int sm, cudaStream_t s)
 {
     const size_t smem = (size_t)bg.tw * bg.th * (8 + 2);
     const int grid = sm * ctas_per_sm;
@@ -255,8 +293,15 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
     prof_end(P_TILE, s);
     prof_begin(P_SEAM, s);
     const int fmax = bg.tw > bg.th ? bg.tw : bg.th;
-    const long long work = (long long)ntiles * 3 * ((fmax + 3) / 4);
-    k_batch_seam<<<grid_for(work, 128, sm), 128, 0, s>>>(node, bg, imgs, tiles, ntiles, err);
+    const long long work = (long long)ntiles * 3 * fmax * forward_offsets(bg.conn).n;
+    if (seam.buckets > 0) {
+        cudaMemsetAsync(seam.count, 0, 4, s);
+        cudaMemsetAsync(seam.hist, 0, 4 * SEAM_BINS, s);
+        k_batch_seam_collect<<<grid_for(work, 256, sm), 256, 0, s>>>(node, bg, imgs, tiles, ntiles, seam);
+        launch_seam_buckets(seam, node, bg.N, err, sm, s);
+    } else {
+        k_batch_seam<<<grid_for(work, 128, sm), 128, 0, s>>>(node, bg, imgs, tiles, ntiles, err);
+    }
     prof_end(P_SEAM, s);
     launch_canon(node, bg, parent, isroot, num_nodes, err, sm, s);
 }

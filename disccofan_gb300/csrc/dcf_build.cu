@@ -49,7 +49,7 @@ __global__ void k_stats(const T *__restrict__ img, long long n, unsigned *kmin, 
 }
 
 template <typename T, bool MIN>
-__global__ void __launch_bounds__(TILE_THREADS)
+__global__ void __launch_bounds__(TILE_THREADS, 5)
 k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__restrict__ gval,
              unsigned long long *__restrict__ gnode, unsigned *err)
 {
@@ -62,65 +62,209 @@ k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__r
 // ---------------------------------------------------------------------------
 // seam merge in HBM
 // ---------------------------------------------------------------------------
-// Seam merge: work item = (tile, face, segment).  Faces are the tile's +x, -x, +y,
-// -y, +z sides (forward offsets never point to -z); a segment is a run of face
-// pixels one thread walks in order, merging every forward edge of each pixel that
-// leaves the tile.  Every cross-tile edge leaves its low endpoint's tile through
-// one of these faces, so all are merged (edges at tile corners possibly twice,
-// which is harmless).
-constexpr int SEAM_SEG = 4;
-
-// largest tile face in SEAM_SEG runs
-__host__ __device__ inline int seam_segments_per_face(const Geom &g)
+// Seam merge.  Work item = (tile, face, face pixel, forward offset).  Faces are the
+// tile's +x, -x, +y, -y, +z sides (forward offsets never point to -z); face f takes
+// the offsets that point out through it (dx = +1 for +x, ...).  Every cross-tile
+// edge leaves its low endpoint's tile through at least one face it points out of,
+// so all are found (corner edges possibly twice, which is harmless).  Each edge is
+// one connect by one thread: on deep trees (high-dynamic-range images) a connect
+// can walk a root path of 10^5 nodes, so no thread may run several in a row.
+__host__ __device__ inline int seam_face_pixels(const Geom &g)
 {
     int f = g.th * g.td;
     f = f > g.tw * g.td ? f : g.tw * g.td;
     if (g.D > 1) f = f > g.tw * g.th ? f : g.tw * g.th;
-    return (f + SEAM_SEG - 1) / SEAM_SEG;
+    return f;
 }
 
-__global__ void k_seam_merge(unsigned long long *gnode, Geom g, int ntx, int nty, int ntz, unsigned *err)
+__host__ __device__ inline long long seam_items(const Geom &g, long long ntiles)
 {
-    const bool is3d = g.D > 1;
+    return ntiles * 5 * seam_face_pixels(g) * forward_offsets(g.conn).n;
+}
+
+// decode work item w into an edge (p, q); false if the item holds none
+__device__ __forceinline__ bool seam_item(const Geom &g, int ntx, int nty, const Offs &offs, int fmax, long long w,
+                                          int &p, int &q)
+{
     const int TW = g.tw, TH = g.th, TD = g.td;
+    const int e = (int)(w % offs.n);
+    long long r = w / offs.n;
+    const int k = (int)(r % fmax);
+    r /= fmax;
+    const int f = (int)(r % 5);
+    const long long tile = r / 5;
+    const int dx = offs.d[e][0], dy = offs.d[e][1], dz = offs.d[e][2];
+    const bool out = f == 0 ? dx > 0 : f == 1 ? dx < 0 : f == 2 ? dy > 0 : f == 3 ? dy < 0 : dz > 0;
+    const int fpix = f <= 1 ? TH * TD : (f <= 3 ? TW * TD : TW * TH);
+    if (!out || k >= fpix || (f == 4 && g.D == 1)) return false;
+    const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
+    const int x0 = tx * TW, y0 = ty * TH, z0 = tz * TD;
+    const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
+    int lx, ly, lz;
+    if (f <= 1) { lx = f == 0 ? wl - 1 : 0; ly = k % TH; lz = k / TH; }
+    else if (f <= 3) { ly = f == 2 ? hl - 1 : 0; lx = k % TW; lz = k / TW; }
+    else { lz = dl - 1; lx = k % TW; ly = k / TW; }
+    if (lx >= wl || ly >= hl || lz >= dl) return false;
+    const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+    const int qx = x + dx, qy = y + dy, qz = z + dz;
+    if (qx < 0 || qx >= g.W || qy < 0 || qy >= g.H || qz >= g.D) return false;
+    p = (int)((long long)z * g.WH + (long long)y * g.W + x);
+    q = (int)((long long)qz * g.WH + (long long)qy * g.W + qx);
+    return true;
+}
+
+// every edge at once
+__global__ void k_seam_direct(unsigned long long *gnode, Geom g, int ntx, int nty, int ntz, unsigned *err)
+{
     GlobalAcc acc{gnode, err, g.N};
     const Offs offs = forward_offsets(g.conn);
-    bool neg_x = false, neg_y = false;
-    for (int e = 0; e < offs.n; e++) {
-        neg_x |= offs.d[e][0] < 0;
-        neg_y |= offs.d[e][1] < 0;
-    }
-    // face f: 0 +x, 1 -x, 2 +y, 3 -y, 4 +z; pixels per face and segments per face
-    const int fpix[5] = {TH * TD, TH * TD, TW * TD, TW * TD, TW * TH};
-    const int nseg_face = seam_segments_per_face(g);
-    const long long ntiles = (long long)ntx * nty * ntz;
-    const long long work = ntiles * 5 * nseg_face;
+    const int fmax = seam_face_pixels(g);
+    const long long work = seam_items(g, (long long)ntx * nty * ntz);
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
          w += (long long)gridDim.x * blockDim.x) {
-        const int sg = (int)(w % nseg_face);
-        const int f = (int)((w / nseg_face) % 5);
-        const long long tile = w / (5LL * nseg_face);
-        if ((f == 1 && !neg_x) || (f == 3 && !neg_y) || (f == 4 && !is3d)) continue;
-        if (sg * SEAM_SEG >= fpix[f]) continue;
-        const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
-        const int x0 = tx * TW, y0 = ty * TH, z0 = tz * TD;
-        const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
-        for (int k = sg * SEAM_SEG; k < min(fpix[f], (sg + 1) * SEAM_SEG); k++) {
-            int lx, ly, lz;
-            if (f <= 1) { lx = f == 0 ? wl - 1 : 0; ly = k % TH; lz = k / TH; }
-            else if (f <= 3) { ly = f == 2 ? hl - 1 : 0; lx = k % TW; lz = k / TW; }
-            else { lz = dl - 1; lx = k % TW; ly = k / TW; }
-            if (lx >= wl || ly >= hl || lz >= dl) continue;
-            const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
-            const int p = (int)((long long)z * g.WH + (long long)y * g.W + x);
-            for (int e = 0; e < offs.n; e++) {
-                int qx = x + offs.d[e][0], qy = y + offs.d[e][1], qz = z + offs.d[e][2];
-                if (qx < 0 || qx >= g.W || qy < 0 || qy >= g.H || qz >= g.D) continue;
-                if (qx >= x0 && qx < x0 + TW && qy >= y0 && qy < y0 + TH && qz >= z0 && qz < z0 + TD) continue;
-                connect(acc, p, (int)((long long)qz * g.WH + (long long)qy * g.W + qx), MERGE_BOUND_GLOBAL);
-            }
-        }
+        int p, q;
+        if (seam_item(g, ntx, nty, offs, fmax, w, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
     }
+}
+
+__global__ void k_seam_collect(const unsigned long long *gnode, Geom g, int ntx, int nty, int ntz, SeamEdges e)
+{
+    const Offs offs = forward_offsets(g.conn);
+    const int fmax = seam_face_pixels(g);
+    const long long work = seam_items(g, (long long)ntx * nty * ntz);
+    const int lane = threadIdx.x & 31;
+    // warp-uniform loop: seam_append is a warp collective
+    for (long long base = blockIdx.x * (long long)blockDim.x + threadIdx.x - lane; base < work;
+         base += (long long)gridDim.x * blockDim.x) {
+        int p = 0, q = 0;
+        const bool valid = base + lane < work && seam_item(g, ntx, nty, offs, fmax, base + lane, p, q);
+        seam_append(e, gnode, valid, p, q);
+    }
+}
+
+long long seam_edge_bound(const Geom &g, long long ntiles)
+{
+    const Offs o = forward_offsets(g.conn);
+    int n[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < o.n; i++) {
+        n[0] += o.d[i][0] > 0;
+        n[1] += o.d[i][0] < 0;
+        n[2] += o.d[i][1] > 0;
+        n[3] += o.d[i][1] < 0;
+        n[4] += o.d[i][2] > 0;
+    }
+    const long long fpix[5] = {(long long)g.th * g.td, (long long)g.th * g.td, (long long)g.tw * g.td,
+                               (long long)g.tw * g.td, (long long)g.tw * g.th};
+    long long per = 0;
+    for (int f = 0; f < 5; f++) per += fpix[f] * n[f];
+    return ntiles * per;
+}
+
+static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+size_t seam_edges_bytes(long long cap, int buckets)
+{
+    return al256(8 * (size_t)cap) * 2 + al256(4 * (size_t)cap) + al256(4 * SEAM_BINS) + al256(2 * SEAM_BINS) +
+           al256(4 * (2 * (size_t)buckets + 1)) + al256(4) + 256;
+}
+
+SeamEdges seam_edges_carve(void *mem, long long cap, int buckets)
+{
+    SeamEdges e;
+    char *m = (char *)mem;
+    auto take = [&](size_t b) { void *p = m; m += al256(b); return p; };
+    e.pq = (int2 *)take(8 * (size_t)cap);
+    e.sorted = (int2 *)take(8 * (size_t)cap);
+    e.lvl = (unsigned *)take(4 * (size_t)cap);
+    e.hist = (unsigned *)take(4 * SEAM_BINS);
+    e.bin_bucket = (unsigned short *)take(2 * SEAM_BINS);
+    e.bstart = (unsigned *)take(4 * (2 * (size_t)buckets + 1));
+    e.count = (unsigned *)take(4);
+    e.cap = cap;
+    e.buckets = buckets;
+    return e;
+}
+
+// Bucket boundaries from the level histogram (one block): bins are assigned in
+// order to buckets of about count / buckets edges; bstart[0..B] is the exclusive
+// prefix of the bucket sizes, bstart[B+1..2B] the scatter counters (zeroed).
+__global__ void __launch_bounds__(1024) k_seam_bounds(SeamEdges e)
+{
+    __shared__ unsigned s_sum[1024];
+    __shared__ unsigned s_bcount[1024];
+    const int t = threadIdx.x, B = e.buckets;
+    const unsigned total = (long long)*e.count < e.cap ? *e.count : (unsigned)e.cap;
+    const unsigned per = total / B + 1;
+    constexpr int PER_T = SEAM_BINS / 1024;
+    unsigned local = 0;
+    for (int j = 0; j < PER_T; j++) local += e.hist[t * PER_T + j];
+    s_sum[t] = local;
+    s_bcount[t] = 0;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan
+        const unsigned v = t >= o ? s_sum[t - o] : 0;
+        __syncthreads();
+        s_sum[t] += v;
+        __syncthreads();
+    }
+    unsigned run = s_sum[t] - local;
+    for (int j = 0; j < PER_T; j++) {
+        const int bin = t * PER_T + j;
+        const unsigned h = e.hist[bin];
+        const unsigned b = min((unsigned)(B - 1), run / per);
+        e.bin_bucket[bin] = (unsigned short)b;
+        if (h) atomicAdd(s_bcount + b, h);
+        run += h;
+    }
+    __syncthreads();
+    if (t == 0) {
+        unsigned acc = 0;
+        for (int b = 0; b < B; b++) {
+            e.bstart[b] = acc;
+            acc += s_bcount[b];
+            e.bstart[B + 1 + b] = 0;
+        }
+        e.bstart[B] = acc;
+    }
+}
+
+__global__ void k_seam_scatter(SeamEdges e)
+{
+    const unsigned total = (long long)*e.count < e.cap ? *e.count : (unsigned)e.cap;
+    const int lane = threadIdx.x & 31;
+    unsigned *fill = e.bstart + e.buckets + 1;
+    for (long long base = blockIdx.x * (long long)blockDim.x + threadIdx.x - lane; base < total;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long i = base + lane;
+        const bool valid = i < total;
+        const unsigned b = valid ? e.bin_bucket[e.lvl[i] >> 16] : 0xFFFFFFFFu;
+        const unsigned same = __match_any_sync(0xffffffffu, b);
+        if (!valid) continue;
+        const int leader = __ffs(same) - 1;
+        unsigned pos = 0;
+        if (lane == leader) pos = atomicAdd(fill + b, (unsigned)__popc(same));
+        pos = __shfl_sync(same, pos, leader);
+        e.sorted[e.bstart[b] + pos + __popc(same & ((1u << lane) - 1u))] = e.pq[i];
+    }
+}
+
+__global__ void k_seam_bucket(SeamEdges e, int b, unsigned long long *gnode, long long n, unsigned *err)
+{
+    GlobalAcc acc{gnode, err, n};
+    const unsigned lo = e.bstart[b], hi = e.bstart[b + 1];
+    for (long long i = lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < hi;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int2 pq = e.sorted[i];
+        connect(acc, pq.x, pq.y, MERGE_BOUND_GLOBAL);
+    }
+}
+
+void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, unsigned *err, int sm, cudaStream_t s)
+{
+    k_seam_bounds<<<1, 1024, 0, s>>>(e);
+    k_seam_scatter<<<grid_for(e.cap, 256, sm), 256, 0, s>>>(e);
+    const int gb = grid_for(e.cap / e.buckets + 1, 128, sm);
+    for (int b = 0; b < e.buckets; b++) k_seam_bucket<<<gb, 128, 0, s>>>(e, b, node, n, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -172,9 +316,16 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
     prof_end(P_TILE, s);
     prof_begin(P_SEAM, s);
     {
-        const int nseg_face = seam_segments_per_face(a.g);
-        const long long work = (long long)grid.x * grid.y * grid.z * 5 * nseg_face;
-        k_seam_merge<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err);
+        const long long work = seam_items(a.g, (long long)grid.x * grid.y * grid.z);
+        if (a.seam.buckets > 0) {
+            SeamEdges e = a.seam;
+            cudaMemsetAsync(e.count, 0, 4, s);
+            cudaMemsetAsync(e.hist, 0, 4 * SEAM_BINS, s);
+            k_seam_collect<<<grid_for(work, 256, a.sm_count), 256, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, e);
+            launch_seam_buckets(e, a.node, a.g.N, a.err, a.sm_count, s);
+        } else {
+            k_seam_direct<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err);
+        }
     }
     prof_end(P_SEAM, s);
     launch_canon(a.node, a.g, a.parent, a.isroot, a.num_nodes, a.err, a.sm_count, s);

@@ -141,8 +141,76 @@ __device__ __forceinline__ uint64_t wmake(uint32_t key, int par)
     return ((uint64_t)key << 32) | (uint32_t)(par == NONE ? 0xFFFFFFFFu : (uint32_t)par);
 }
 
-// Level root of i (follows equal-key links); on return i is the root and w its word.
-// Path halving shortcuts equal-key links while walking.
+// Read-only level-root walk for the final canonicalisation passes: there every
+// thread writes only its own entry, because a path-halving write from another
+// thread could land after a fully compressed one and undo it.
+template <class A>
+__device__ __forceinline__ int levelroot_ro(A &acc, int i)
+{
+    uint64_t w = acc.load(i);
+    const uint32_t k = wkey(w);
+    const long long bound = acc.walk_bound();
+    for (long long it = 0; it < bound; it++) {
+        const int p = wpar(w);
+        if (p == NONE) return i;
+        const uint64_t wp = acc.load(p);
+        if (wkey(wp) != k) return i;
+        i = p;
+        w = wp;
+    }
+    acc.error(DEVERR_WALK_BOUND);
+    return i;
+}
+
+// Level root of i given its word w, continuing past equal-key links (with path
+// halving); on return (i, w) is the level root and (ni, nw) the first pixel of
+// the parent node and its word (ni = NONE at a root).  The parent's word is the
+// one this walk had to load anyway to see the key change, so a caller stepping
+// down a chain pays one dependent load per node.
+template <class A>
+__device__ __forceinline__ void levelroot_next(A &acc, int &i, uint64_t &w, int &ni, uint64_t &nw)
+{
+    const uint32_t k = wkey(w);
+    const long long bound = acc.walk_bound();
+    for (long long it = 0; it < bound; it++) {
+        const int p = wpar(w);
+        if (p == NONE) {
+            ni = NONE;
+            return;
+        }
+        const uint64_t wp = acc.load(p);
+        if (wkey(wp) != k) {
+            ni = p;
+            nw = wp;
+            return;
+        }
+        const int pp = wpar(wp);
+        if (pp == NONE) {
+            i = p;
+            w = wp;
+            ni = NONE;
+            return;
+        }
+        const uint64_t wpp = acc.load(pp);
+        if (wkey(wpp) == k) {
+            acc.store(i, wmake(k, pp));
+            i = pp;
+            w = wpp;
+            continue;
+        }
+        i = p;
+        w = wp;
+        ni = pp;
+        nw = wpp;
+        return;
+    }
+    ni = NONE;
+    acc.error(DEVERR_WALK_BOUND);
+}
+
+// Level root of i (follows equal-key links, path halving); on return i is the root
+// and w its word.  Used by connect_smem, where a second load per step is cheaper
+// than the registers that carrying the parent's word costs.
 template <class A>
 __device__ __forceinline__ void levelroot(A &acc, int &i, uint64_t &w)
 {
@@ -171,29 +239,11 @@ __device__ __forceinline__ void levelroot(A &acc, int &i, uint64_t &w)
     acc.error(DEVERR_WALK_BOUND);
 }
 
-// Read-only level-root walk for the final canonicalisation passes: there every
-// thread writes only its own entry, because a path-halving write from another
-// thread could land after a fully compressed one and undo it.
+// connect() for node words in shared memory (the in-tile merge): the same splices,
+// re-reading a parent's word at every step (shared-memory latency is a few tens of
+// cycles) to keep the tile kernel's register count, and so its occupancy, down.
 template <class A>
-__device__ __forceinline__ int levelroot_ro(A &acc, int i)
-{
-    uint64_t w = acc.load(i);
-    const uint32_t k = wkey(w);
-    const long long bound = acc.walk_bound();
-    for (long long it = 0; it < bound; it++) {
-        const int p = wpar(w);
-        if (p == NONE) return i;
-        const uint64_t wp = acc.load(p);
-        if (wkey(wp) != k) return i;
-        i = p;
-        w = wp;
-    }
-    acc.error(DEVERR_WALK_BOUND);
-    return i;
-}
-
-template <class A>
-__device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
+__device__ __forceinline__ void connect_smem(A &acc, int a, int b, long long bound)
 {
     uint64_t wa, wb;
     levelroot(acc, a, wa);
@@ -206,14 +256,13 @@ __device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
             uint64_t tw = wa; wa = wb; wb = tw;
             uint32_t tk = ka; ka = kb; kb = tk;
         }
-        // a sits above b: ka > kb, or equal keys with a > b (a's node joins b's)
         const int pa = wpar(wa);
         int lpa = pa;
         uint64_t wl = 0;
         if (pa != NONE) {
             levelroot(acc, lpa, wl);
             if (lpa == b) return;
-            if (wkey(wl) >= kb) {  // b belongs below a's parent node: descend
+            if (wkey(wl) >= kb) {
                 a = lpa;
                 wa = wl;
                 continue;
@@ -221,7 +270,6 @@ __device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
         }
         if (acc.cas(a, wa, wmake(ka, b))) {
             if (pa == NONE) return;
-            // merge the displaced tail (a's old parent node) into b's chain
             a = b;
             wa = wb;
             b = lpa;
@@ -229,6 +277,61 @@ __device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
         } else {
             levelroot(acc, a, wa);
             levelroot(acc, b, wb);
+        }
+    }
+    acc.error(DEVERR_MERGE_BOUND);
+}
+
+// Every (x, wx) pair below is read in the order word of x, then word of its parent
+// (nx, nwx); a pair may be older than other threads' writes, like the view of a
+// delayed thread, and structure only changes through a CAS on the exact word held.
+template <class A>
+__device__ __forceinline__ void connect(A &acc, int a, int b, long long bound)
+{
+    uint64_t wa = acc.load(a), wb = acc.load(b), nwa = 0, nwb = 0;
+    int na, nb;
+    levelroot_next(acc, a, wa, na, nwa);
+    levelroot_next(acc, b, wb, nb, nwb);
+    for (long long it = 0; it < bound; it++) {
+        if (a == b) return;
+        uint32_t ka = wkey(wa), kb = wkey(wb);
+        if (ka < kb || (ka == kb && a < b)) {
+            int t = a; a = b; b = t;
+            uint64_t tw = wa; wa = wb; wb = tw;
+            t = na; na = nb; nb = t;
+            tw = nwa; nwa = nwb; nwb = tw;
+            uint32_t tk = ka; ka = kb; kb = tk;
+        }
+        // a sits above b: ka > kb, or equal keys with a > b (a's node joins b's)
+        int lpa = na, nl = NONE;
+        uint64_t wl = nwa, nwl = 0;
+        if (na != NONE) {
+            levelroot_next(acc, lpa, wl, nl, nwl);
+            if (lpa == b) return;
+            if (wkey(wl) >= kb) {  // b belongs below a's parent node: descend
+                a = lpa;
+                wa = wl;
+                na = nl;
+                nwa = nwl;
+                continue;
+            }
+        }
+        if (acc.cas(a, wa, wmake(ka, b))) {
+            if (na == NONE) return;
+            // merge the displaced tail (a's old parent node) into b's chain
+            a = b;
+            wa = wb;
+            na = nb;
+            nwa = nwb;
+            b = lpa;
+            wb = wl;
+            nb = nl;
+            nwb = nwl;
+        } else {
+            wa = acc.load(a);
+            levelroot_next(acc, a, wa, na, nwa);
+            wb = acc.load(b);
+            levelroot_next(acc, b, wb, nb, nwb);
         }
     }
     acc.error(DEVERR_MERGE_BOUND);

@@ -28,6 +28,34 @@ inline int grid_for(long long n, int block, int sm_count)
     return (int)b;
 }
 
+// Seam merge of tile forests.  The cross-tile edges are collected with their level
+// min(key p, key q); with buckets > 0 they are merged in ascending level order, in
+// `buckets` ranges of about equal size: the lowest edges zip the long root paths
+// (trunks) of neighbouring tiles first, so later, higher edges stop where the chains
+// are already one instead of each walking the trunk again.  buckets == 0 merges
+// every edge at once, one connect per thread.  A collect kernel (one per
+// enumeration: whole image or batch) appends the edges and histograms the levels'
+// top 16 bits; launch_seam_buckets splits and merges them.
+constexpr int SEAM_BINS = 65536;
+struct SeamEdges {
+    int2 *pq = nullptr;              // collected edges (capacity cap)
+    unsigned *lvl = nullptr;
+    int2 *sorted = nullptr;          // edges grouped by bucket
+    unsigned *hist = nullptr;        // SEAM_BINS counts of level >> 16
+    unsigned short *bin_bucket = nullptr;  // SEAM_BINS
+    unsigned *bstart = nullptr;      // buckets + 1 (exclusive prefix), then the buckets' fill counters
+    unsigned *count = nullptr;
+    long long cap = 0;
+    int buckets = 0;
+};
+// layout for up to `buckets` buckets (e.buckets may later be set to any value up to it)
+size_t seam_edges_bytes(long long cap, int buckets);
+SeamEdges seam_edges_carve(void *mem, long long cap, int buckets);
+// bound on the cross-tile edges of a tile grid (outward offsets per face)
+long long seam_edge_bound(const Geom &g, long long ntiles);
+void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, unsigned *err, int sm_count,
+                         cudaStream_t s);
+
 struct BuildArgs {
     int dtype;
     bool tree_min;
@@ -41,14 +69,14 @@ struct BuildArgs {
     unsigned long long *num_nodes;
     unsigned *err;
     int sm_count;
+    SeamEdges seam;                  // level-ordered seam merge scratch (buckets == 0: direct merge)
 };
+void launch_canon(unsigned long long *node, const Geom &g, int *parent, unsigned char *isroot,
+                  unsigned long long *num_nodes, unsigned *err, int sm_count, cudaStream_t s);
 
 void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsigned *kmax, unsigned *nans,
                   int sm_count, cudaStream_t s);
 void launch_build(const BuildArgs &a, cudaStream_t s);
-// canonical form of the merged node words (pixel -> level root, root -> parent's level root)
-void launch_canon(unsigned long long *node, const Geom &g, int *parent, unsigned char *isroot,
-                  unsigned long long *num_nodes, unsigned *err, int sm_count, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // batches of 2-D cutouts: pixels of all cutouts concatenated, cutout i at element
@@ -67,7 +95,9 @@ struct BatchTile {
 void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchImg *imgs, const BatchTile *tiles,
                         int ntiles, int chunk, unsigned *next, float *gval, unsigned long long *node, int *parent,
                         unsigned char *isroot, unsigned long long *num_nodes, unsigned *err, int ctas_per_sm,
-                        int sm_count, cudaStream_t s);
+                        SeamEdges &seam, int sm_count, cudaStream_t s);
+// bound on a batch's cross-tile edges (capacity of its SeamEdges)
+long long batch_seam_edge_bound(const Geom &bg, const BatchImg *imgs_host, int count);
 
 // ---------------------------------------------------------------------------
 // attribute records (structure of arrays over pixels; valid at level roots)

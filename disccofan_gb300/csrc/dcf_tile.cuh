@@ -107,7 +107,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
                     if (!crosses) continue;
                     int qx = lx - dx, qy = ly - dy, qz = lz - dz;
                     if (qx < 0 || qx >= wl || qy < 0 || qy >= hl || qz < 0 || qz >= dl) continue;
-                    connect(acc, p, qx + qy * TW + qz * TW * TH, MERGE_BOUND_SMEM);
+                    connect_smem(acc, p, qx + qy * TW + qz * TW * TH, MERGE_BOUND_SMEM);
                 }
             }
             // levels are ordered for shorter merge walks, not for correctness:
@@ -155,5 +155,33 @@ struct GlobalAcc {
     __device__ long long walk_bound() const { return n + 1; }
     __device__ void error(unsigned bit) { raise_error(err, bit); }
 };
+
+// Appends one cross-tile edge (p, q) with its level min(key p, key q) to e;
+// warp-aggregated counter and histogram atomics.  A warp collective: every lane
+// calls it, `valid` says whether the lane has an edge.
+__device__ __forceinline__ void seam_append(SeamEdges &e, const unsigned long long *gnode, bool valid, int p, int q)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned lvl = 0;
+    if (valid) {
+        const unsigned kp = wkey(((const volatile unsigned long long *)gnode)[p]);
+        const unsigned kq = wkey(((const volatile unsigned long long *)gnode)[q]);
+        lvl = kp < kq ? kp : kq;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, valid);
+    if (!m) return;
+    unsigned base = 0;
+    if (lane == __ffs(m) - 1) base = atomicAdd(e.count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+    const unsigned bin = valid ? lvl >> 16 : 0xFFFFFFFFu;
+    const unsigned same = __match_any_sync(0xffffffffu, bin);
+    if (!valid) return;
+    if (lane == __ffs(same) - 1) atomicAdd(e.hist + bin, (unsigned)__popc(same));
+    const unsigned i = base + __popc(m & ((1u << lane) - 1u));
+    if ((long long)i < e.cap) {
+        e.pq[i] = make_int2(p, q);
+        e.lvl[i] = lvl;
+    }
+}
 
 }  // namespace dcf

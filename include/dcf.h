@@ -181,14 +181,19 @@ typedef struct {
 dcf_status dcf_batch_create(dcf_ctx *ctx, int count, const uint32_t *widths, const uint32_t *heights, int dtype,
                             int connectivity, int attr_idx, const float *pixdim, dcf_batch **out);
 dcf_status dcf_batch_destroy(dcf_batch *batch);
-/* schedule[4] = tile width, tile height, CTAs per SM, tiles per queue grab;
- * graph_kernels = kernel nodes in the recorded graph (0: none recorded) */
+/* schedule[6] = tile width, tile height, CTAs per SM, tiles per queue grab, seam
+ * buckets, bottom-up steps; graph_kernels = kernel nodes of the last graph launched */
 dcf_status dcf_batch_info(const dcf_batch *batch, uint64_t *total_pixels, uint64_t *num_nodes, int *schedule,
                           uint64_t *graph_kernels);
 /* Persistent tile-build schedule (ctas_per_sm <= 0: as many as fit). */
 dcf_status dcf_batch_set_schedule(dcf_ctx *ctx, dcf_batch *batch, int tile_w, int tile_h, int ctas_per_sm, int chunk);
-/* Time the build phase over tile shapes, then CTAs per SM and queue chunk for the
- * best shape, on these pixels; keep the fastest schedule.  Leaves no valid trees. */
+/* Tree-merge parameters: seam_buckets = number of ascending-level ranges the seam
+ * edges are merged in (0 = all at once; at most 256); up_steps = bottom-up fold
+ * steps per walker before the remaining nodes are finished by pointer jumping. */
+dcf_status dcf_batch_set_merge(dcf_ctx *ctx, dcf_batch *batch, int seam_buckets, int up_steps);
+/* Time, on these pixels, the build over tile shapes, then CTAs per SM and queue
+ * chunk for the best shape, then seam buckets, then build + attributes over
+ * bottom-up steps; keep the fastest of each.  Leaves no valid trees. */
 dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *batch, const void *pixels, int on_device, int repeats,
                               double *best_ms);
 /* Build every cutout's tree and attributes, then the requested operations:

@@ -106,11 +106,15 @@ def test_batch_schedules_agree():
     b = ctx.batch(shapes, np.uint16, connectivity=8, attribute=13)
     pix = b.concat(cuts)
     first = None
-    for tile, ctas, chunk in (((64, 64), 0, 1), ((32, 32), 1, 4), ((16, 64), 2, 2), ((128, 16), 0, 8),
-                              ((64, 32), 3, 1)):
+    # tile shape, CTAs per SM, queue chunk, seam buckets, bottom-up steps
+    for tile, ctas, chunk, buckets, up in (((64, 64), 0, 1, 16, 2048), ((32, 32), 1, 4, 0, 7),
+                                           ((16, 64), 2, 2, 64, 100000), ((128, 16), 0, 8, 3, 2048),
+                                           ((64, 32), 3, 1, 256, 0)):
         b.set_schedule(tile, ctas, chunk)
+        b.set_merge(seam_buckets=buckets, up_steps=up)
         info = b.info()
         assert info["tile"] == tile and info["chunk"] == chunk
+        assert info["seam_buckets"] == buckets and info["up_steps"] == up
         f, s = b.run(pix, filter_attr=0, lam=50.0, spectrum=spec_ops(), use_graph=False)
         par = b.parent()
         if first is None:
