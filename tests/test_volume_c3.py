@@ -11,8 +11,6 @@ divides by pow(volume, 5/3), evaluated to within an ulp of glibc).  The smaller
 volume also covers the operations built from the filter: extract, the differential
 morphological profile and the attribute check.
 """
-import os
-
 import numpy as np
 import pytest
 
@@ -38,7 +36,9 @@ def lognormal_volume(n, seed=3, sigma=6.0):
 @pytest.mark.parametrize("n", [64, 256])
 def test_lognormal_volume_against_oracle(ctx, n):
     vol = lognormal_volume(n)
-    port = oracle.Port(threads=os.cpu_count() or 1)
+    # one oracle thread: with several, like the reference under OpenMP, level roots
+    # inside flat zones (float32 ties) are not the canonical lowest index
+    port = oracle.Port(threads=1)
     port.load(vol, 6, "max")
     port.prepare(17)
     t = ctx.build(vol, connectivity=6, tree_type="max", attribute=17)
