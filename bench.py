@@ -266,7 +266,7 @@ def run_ours(args):
     total_prof = sum(v[0] for v in prof.values())
     M = sum(node_counts) / 2.0
     per_launch = {
-        "tile_build": npix * (s_in + 4),            # image in, parent out
+        "tile_build": npix * (s_in + 4 + 8),        # image in; level and node word out
         "seam_merge": npix * (4 + 4) * 0.047,       # shell pixels: parent + level read (2-D, 64x64 tiles)
         "canonicalise": npix * (4 + 4 + 1),         # parent read+write, root flag
         "attr_pixels": npix * (4 + 1) + M * 12,     # parent + root flag in, area+bbox records out
@@ -279,6 +279,13 @@ def run_ours(args):
         "stats": npix * s_in,
     }
     alg = per_launch.get(dom, npix * s_in)
+    # DRAM bytes per pixel per launch from one ncu capture of the kernel on a
+    # 4096^2 uint16 image (profiles/k_tile_build_4096_u16.md,
+    # profiles/k_seam_direct_4096_u16.md), scaled by pixels: traffic grows with
+    # the pixel count for these per-pixel passes
+    dram_per_px = {"tile_build": (34.657024e6 + 155.2128e6) / 4096 ** 2,
+                   "seam_merge": (133.971456e6 + 74.045184e6) / 4096 ** 2}
+    traffic = round(dram_per_px[dom] * npix) if dom in dram_per_px else None
     achieved = alg / (dom_ms / dom_n * 1e-3) / 1e9
     B_alg = 2 * (npix * (s_in + 4 + s_in) + 12 * M) + 2 * 8 * 441
     result = {
@@ -304,7 +311,8 @@ def run_ours(args):
                                          "frac": round(B_alg / (ms * 1e-3) / 1e9 / peak, 5)},
                    "kernel_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sorted(prof.items())}},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": None,
+                     "frac": round(achieved / peak, 5), "traffic": traffic,
+                     "traffic_source": "ncu DRAM read+write of one 4096^2 launch, scaled by pixels",
                      "share": round(dom_ms / total_prof, 4) if total_prof else None,
                      "alg_bytes_per_launch": alg, "peak_source": f"{peak_kind} hbm_gbs"},
         "e2e": {"value": round(world * npix / 1e6 / (e2e_ms * 1e-3), 3), "unit": "Mpx/s",

@@ -235,7 +235,8 @@ dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out)
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (const char *e = getenv("DCF_TILE2D")) {  // e.g. "32x32"
         int a = 0, b = 0;
-        if (sscanf(e, "%dx%d", &a, &b) == 2 && a > 0 && b > 0 && a * b <= TILE_MAX_PIX) {
+        if (sscanf(e, "%dx%d", &a, &b) == 2 && a > 0 && b > 0 && a * b <= TILE_MAX_PIX &&
+            tile_smem_bytes(a, b, 1) <= 48 * 1024) {
             ctx->tile2d[0] = a;
             ctx->tile2d[1] = b;
         }
@@ -1042,8 +1043,9 @@ static constexpr int SEAM_BUCKETS_MAX = 256;
 
 static dcf_status batch_set_tiles(dcf_ctx *ctx, dcf_batch *b, int tw, int th, int ctas, int chunk)
 {
-    if (tw < 1 || th < 1 || tw * th > TILE_MAX_PIX)
-        return set_err(ctx, DCF_ERR_INVALID, "tile %dx%d (at most %d pixels)", tw, th, TILE_MAX_PIX);
+    if (tw < 1 || th < 1 || tw * th > TILE_MAX_PIX || tile_smem_bytes(tw, th, 1) > 48 * 1024)
+        return set_err(ctx, DCF_ERR_INVALID, "tile %dx%d (at most %d pixels, 48 KiB of shared memory)", tw, th,
+                       TILE_MAX_PIX);
     const int maxc = batch_max_ctas_per_sm(b->dtype, tw, th);
     if (maxc < 1) return set_err(ctx, DCF_ERR_INVALID, "tile %dx%d does not fit on an SM", tw, th);
     if (ctas < 1 || ctas > maxc) ctas = maxc;

@@ -276,7 +276,7 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
                         unsigned char *isroot, unsigned long long *num_nodes, unsigned *err, int ctas_per_sm,
                         SeamEdges &seam, int sm, cudaStream_t s)
 {
-    const size_t smem = (size_t)bg.tw * bg.th * (8 + 2);
+    const size_t smem = tile_smem_bytes(bg.tw, bg.th, 1);
     const int grid = sm * ctas_per_sm;
     cudaMemsetAsync(next, 0, sizeof(unsigned), s);
     prof_begin(P_TILE, s);
@@ -350,7 +350,7 @@ namespace dcf {
 // CTAs of the persistent tile kernel that fit on one SM for a tile shape
 int batch_max_ctas_per_sm(int dtype, int tw, int th)
 {
-    const size_t smem = (size_t)tw * th * (8 + 2);
+    const size_t smem = tile_smem_bytes(tw, th, 1);
     int n = 0;
     switch (dtype) {
     case U8: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_tile_build<uint8_t>, TILE_THREADS, smem); break;

@@ -310,7 +310,7 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
     const T *img = (const T *)a.img;
     const int TW = a.g.tw, TH = a.g.th, TD = a.g.td;
     dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
-    const size_t smem = (size_t)TW * TH * TD * (8 + 2);
+    const size_t smem = tile_smem_bytes(TW, TH, TD);
     prof_begin(P_TILE, s);
     k_tile_build<T, MIN><<<grid, TILE_THREADS, smem, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err);
     prof_end(P_TILE, s);

@@ -19,6 +19,12 @@ constexpr int TILE_MAX_PIX = 4096;             // largest build tile (16-bit loc
 constexpr long long MERGE_BOUND_SMEM = 1LL << 22;
 constexpr long long MERGE_BOUND_GLOBAL = 1LL << 28;
 
+// dynamic shared memory of one tile build (padded node words + padded row stacks)
+inline size_t tile_smem_bytes(int tw, int th, int td)
+{
+    return (size_t)(tw + 1) * th * td * 8 + (size_t)(tw + 2) * th * td * 2;
+}
+
 inline int grid_for(long long n, int block, int sm_count)
 {
     long long b = (n + block - 1) / block;

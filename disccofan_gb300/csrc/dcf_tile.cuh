@@ -22,9 +22,14 @@ struct SmemAcc {
 
 // Max-tree of one tile by the whole CTA.  The tile starts at (x0, y0, z0) of an
 // image of geometry g whose pixel (x, y, z) has global index off + z*WH + y*W + x
-// (off > 0 for one cutout of a batch).  smem holds tw*th*td node words followed by
-// the row stacks.  Writes gval and the tile forest (level-root form, global
-// indices) into gnode.
+// (off > 0 for one cutout of a batch).  Writes gval and the tile forest
+// (level-root form, global indices) into gnode.
+//
+// Shared-memory layout (tile_smem_bytes): node words with a padded row stride
+// RS = tw + 1 (local index of pixel (lx, ly, lz) = lx + ly*RS + lz*RS*th), then one
+// stack per row with stride tw + 2 entries.  The row pass runs one row per thread
+// in lock-step; unpadded strides of tw words would put all 32 rows of a warp in
+// the same shared-memory bank at every step.
 template <typename T, bool MIN>
 __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long off, const Geom &g, int x0, int y0,
                                            int z0, float gmax, float *__restrict__ gval,
@@ -33,14 +38,15 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
 {
     // tile extents from the geometry (at most 4096 pixels: local indices < 2^16)
     const bool is3d = g.D > 1;
-    const int TW = g.tw, TH = g.th, TD = g.td, TILE_PIX = TW * TH * TD;
-    unsigned long long *snode = smem_tile;                               // TILE_PIX words
-    unsigned short *sstk = (unsigned short *)(smem_tile + TILE_PIX);     // one TW-long stack per row
+    const int TW = g.tw, TH = g.th, TD = g.td;
+    const int RS = TW + 1, SS = TW + 2, SLICE = RS * TH, WORDS = RS * TH * TD;
+    unsigned long long *snode = smem_tile;                            // WORDS node words
+    unsigned short *sstk = (unsigned short *)(smem_tile + WORDS);     // one stack per row
     const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
     const int tid = threadIdx.x;
 
-    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
-        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
+    for (int i = tid; i < WORDS; i += TILE_THREADS) {
+        int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         uint32_t k = 0;
         if (lx < wl && ly < hl && lz < dl) {
             long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
@@ -58,9 +64,9 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     for (int r = tid; r < nrows; r += TILE_THREADS) {
         int ly = r % TH, lz = r / TH;
         if (ly >= hl || lz >= dl) continue;
-        unsigned short *stk = sstk + r * TW;
+        unsigned short *stk = sstk + r * SS;
         int sp = 0;
-        const int base = r * TW;
+        const int base = r * RS;
         for (int lx = 0; lx < wl; lx++) {
             int i = base + lx;
             uint32_t ki = wkey(snode[i]);
@@ -77,7 +83,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     }
     __syncthreads();
 
-    SmemAcc acc{snode, err, TILE_PIX};
+    SmemAcc acc{snode, err, WORDS};
     const Offs offs = forward_offsets(g.conn);
     // merge row bands along y (each z slice), then slabs along z; at level k the
     // seams are the rows (slices) c with c % 2^(k+1) == 2^k
@@ -99,7 +105,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
                 if (axis == 1) { ly = c; lz = o; }
                 else { lz = c; ly = o; }
                 if (lx >= wl || ly >= hl || lz >= dl) continue;
-                int p = lx + ly * TW + lz * TW * TH;
+                int p = lx + ly * RS + lz * SLICE;
                 // edges from p to the previous row / slice: the reversed forward offsets
                 for (int e = 0; e < offs.n; e++) {
                     int dx = offs.d[e][0], dy = offs.d[e][1], dz = offs.d[e][2];
@@ -107,7 +113,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
                     if (!crosses) continue;
                     int qx = lx - dx, qy = ly - dy, qz = lz - dz;
                     if (qx < 0 || qx >= wl || qy < 0 || qy >= hl || qz < 0 || qz >= dl) continue;
-                    connect_smem(acc, p, qx + qy * TW + qz * TW * TH, MERGE_BOUND_SMEM);
+                    connect_smem(acc, p, qx + qy * RS + qz * SLICE, MERGE_BOUND_SMEM);
                 }
             }
             // levels are ordered for shorter merge walks, not for correctness:
@@ -119,14 +125,14 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
 
     // level-root form inside the tile (read-only walks, then each pixel writes its
     // own word): pixel -> level root, root -> parent's level root; to global indices
-    unsigned short *sroot = sstk;  // the row stacks are no longer needed
-    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
-        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
+    unsigned short *sroot = sstk;  // the row stacks (>= WORDS entries) are no longer needed
+    for (int i = tid; i < WORDS; i += TILE_THREADS) {
+        int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         sroot[i] = (lx < wl && ly < hl && lz < dl) ? (unsigned short)levelroot_ro(acc, i) : (unsigned short)0xFFFFu;
     }
     __syncthreads();
-    for (int i = tid; i < TILE_PIX; i += TILE_THREADS) {
-        int lx = i % TW, ly = (i / TW) % TH, lz = i / (TW * TH);
+    for (int i = tid; i < WORDS; i += TILE_THREADS) {
+        int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         if (lx >= wl || ly >= hl || lz >= dl) continue;
         const uint64_t w = snode[i];
         int p = sroot[i];
@@ -136,7 +142,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
         }
         int out = NONE;
         if (p != NONE) {
-            int px = p % TW, py = (p / TW) % TH, pz = p / (TW * TH);
+            int px = p % RS, py = (p / RS) % TH, pz = p / SLICE;
             out = (int)(off + (long long)(z0 + pz) * g.WH + (long long)(y0 + py) * g.W + (x0 + px));
         }
         long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
