@@ -401,10 +401,21 @@ def run_batch(args, ctx, stream):
     spec = (13, l_tr, 0, l_ar)
     b = ctx.batch(shapes, np.float32, connectivity=8, attribute=13)
     spectra = torch.empty((len(shapes), l_ar.size, l_tr.size), dtype=torch.float64, device="cuda")
+    # the schedule is tuned on a sample batch (the first tune_n cutouts) and applied
+    # to the whole batch, so that tuning stays within seconds
+    tune_n = min(len(shapes), args.tune_sample)
     t0 = time.perf_counter()
-    tune_ms = b.autotune(pix, repeats=1) if not args.no_autotune else None
+    tune_ms = None
+    if not args.no_autotune:
+        tb = ctx.batch(shapes[:tune_n], np.float32, connectivity=8, attribute=13)
+        tune_px = sum(h * w for h, w in shapes[:tune_n])
+        tune_ms = tb.autotune(pix[:tune_px], repeats=1)
+        ti = tb.info()
+        tb.close()
+        b.set_schedule(ti["tile"], ti["ctas_per_sm"], ti["chunk"])
+        b.set_merge(ti["seam_buckets"], ti["up_steps"])
     tune_s = time.perf_counter() - t0
-    log(f"batch: autotuned in {tune_s:.1f}s -> {b.info()}")
+    log(f"batch: autotuned on {tune_n} cutouts in {tune_s:.1f}s -> {b.info()}")
     for _ in range(max(args.warmup, 2)):  # learns the capacity, then records the graph
         b.run(pix, spectrum=spec, use_graph=True, spectra=spectra)
     torch.cuda.synchronize()
@@ -456,7 +467,8 @@ def run_batch(args, ctx, stream):
             "speedup_vs_loop": round(loop_ms / graph_ms, 2), "max_rel_spectrum_diff_vs_loop": diff,
             "loop_sample": f"first {loop_n} cutouts ({loop_px} px), one pass, scaled to the batch's pixels",
             "schedule": {"tile": info["tile"], "ctas_per_sm": info["ctas_per_sm"], "chunk": info["chunk"]},
-            "autotune": {"best_build_ms": None if tune_ms is None else round(tune_ms, 3), "seconds": round(tune_s, 2)},
+            "autotune": {"sample_cutouts": tune_n, "best_sample_build_ms": None if tune_ms is None else round(tune_ms, 3),
+                         "seconds": round(tune_s, 2), "seam_buckets": info["seam_buckets"], "up_steps": info["up_steps"]},
             "graph_kernels": info["graph_kernels"], "gpu_launches_per_step": int(graph_launches), "steps": steps}
 
 
@@ -624,6 +636,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="batched workload: keep the default schedule")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--loop-sample", type=int, default=512, help="cutouts timed through the single-image API")
+    ap.add_argument("--tune-sample", type=int, default=512, help="cutouts the batch schedule is tuned on")
     ap.add_argument("--adj-count", type=int, default=256)
     args = ap.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -82,6 +82,10 @@ static void prof_record(int id, bool begin, cudaStream_t s)
 namespace dcf {
 void prof_begin(int id, cudaStream_t s) { prof_record(id, true, s); }
 void prof_end(int id, cudaStream_t s) { prof_record(id, false, s); }
+void note_launch()
+{
+    if (t_active) t_active->launches++;
+}
 }  // namespace dcf
 
 // fold recorded event pairs into per-kernel totals
@@ -144,9 +148,8 @@ static dcf_status set_err(dcf_ctx *c, dcf_status s, const char *fmt, ...)
                                               "%s: %s", #call, cudaGetErrorString(_e));                  \
     } while (0)
 
-static dcf_status check_launch(dcf_ctx *ctx, int nlaunch)
+static dcf_status check_launch(dcf_ctx *ctx, int)
 {
-    ctx->launches += (uint64_t)nlaunch;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_err(ctx, DCF_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
     return DCF_OK;
@@ -645,7 +648,7 @@ dcf_status dcf_tree_parent(dcf_ctx *ctx, dcf_tree *t, int64_t *parent, int on_de
         if (st != DCF_OK) return st;
         dst = (long long *)s;
     }
-    k_widen<<<grid_for(t->g.N, 256, ctx->sm_count), 256, 0, ctx->stream>>>(t->g.N, t->parent, dst);
+    k_widen<<<grid_for(t->g.N, 256, ctx->sm_count), 256, 0, ctx->stream>>>(t->g.N, t->parent, dst); note_launch();
     dcf_status st = check_launch(ctx, 1);
     if (st != DCF_OK) return st;
     if (!on_device) CU(cudaMemcpyAsync(parent, dst, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1625,7 +1628,7 @@ dcf_status dcf_batch_parent(dcf_ctx *ctx, dcf_batch *b, int64_t *parent, int on_
         dst = (long long *)sbuf;
     }
     k_batch_local_parent<<<grid_for(b->N, 256, ctx->sm_count), 256, 0, ctx->stream>>>(b->N, b->parent, b->d_offs,
-                                                                                      b->count, dst);
+                                                                                      b->count, dst); note_launch();
     if ((st = check_launch(ctx, 1)) != DCF_OK) return st;
     if (!on_device) CU(cudaMemcpyAsync(parent, dst, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
     return sync_and_check(ctx);

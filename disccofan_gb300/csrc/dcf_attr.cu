@@ -100,7 +100,7 @@ __global__ void k_fill_u32(long long n, uint32_t *dst, uint32_t v)
 
 void launch_fill_u32(long long n, uint32_t *dst, uint32_t v, int sm, cudaStream_t s)
 {
-    k_fill_u32<<<grid_for(n, 256, sm), 256, 0, s>>>(n, dst, v);
+    k_fill_u32<<<grid_for(n, 256, sm), 256, 0, s>>>(n, dst, v); note_launch();
 }
 
 __global__ void k_mark_leaves(long long n, const unsigned char *__restrict__ isroot, int *pending)
@@ -361,12 +361,12 @@ void launch_attributes_up(const TreeView &t, AttrBufs &a, unsigned *count, int u
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_ATTR_UP, s);
-    k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending);
-#define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, up_steps, err)
+    k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending); note_launch();
+#define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, up_steps, err); note_launch()
     DCF_GROUP_SWITCH(DCF_UP)
 #undef DCF_UP
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, nullptr, count, 0u, err);
+    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, nullptr, count, 0u, err); note_launch();
     prof_end(P_ATTR_UP, s);
 }
 
@@ -374,7 +374,7 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_s
                        cudaStream_t s)
 {
     const int nb = grid_for(t.g.N, 256, sm);
-#define DCF_PIX(G, E) k_attr_pixels<G, E><<<nb, 256, 0, s>>>(t.gval, t.g, t.parent, t.isroot, a)
+#define DCF_PIX(G, E) k_attr_pixels<G, E><<<nb, 256, 0, s>>>(t.gval, t.g, t.parent, t.isroot, a); note_launch()
     prof_begin(P_ATTR_PIX, s);
     DCF_GROUP_SWITCH(DCF_PIX)
 #undef DCF_PIX
@@ -400,23 +400,26 @@ static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool exact,
     m += (4 * (size_t)cap + 255) / 256 * 256;
     RestRecs r0 = carve(m, a.group, cap), r1 = carve(m, a.group, cap);
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, list, count, cap, err);
+    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, list, count, cap, err); note_launch();
     if (cap == 0) return;
     const int rb = grid_for(cap, 256, sm);
-    k_rest_gather<G><<<rb, 256, 0, s>>>(list, count, cap, t.parent, a.pending, a, r0, j0, err);
-    k_rest_links<G><<<rb, 256, 0, s>>>(list, count, cap, t.parent, a.pending, j0, err);
+    k_rest_gather<G><<<rb, 256, 0, s>>>(list, count, cap, t.parent, a.pending, a, r0, j0, err); note_launch();
+    k_rest_links<G><<<rb, 256, 0, s>>>(list, count, cap, t.parent, a.pending, j0, err); note_launch();
     int rounds = 0;
     while ((1u << rounds) < cap && rounds < 31) rounds++;
     RestRecs *ri = &r0, *ro = &r1;
     int *ji = j0, *jo = j1;
     for (int k = 0; k < rounds; k++) {
         if (exact) copy_recs(*ro, *ri, G, cap, s);
-        else k_copy_recs<G><<<rb, 256, 0, s>>>(count, cap, *ri, *ro);
-        k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, cap, ji, jo, *ri, *ro, a.has_z);
+        else {
+            k_copy_recs<G><<<rb, 256, 0, s>>>(count, cap, *ri, *ro);
+            note_launch();
+        }
+        k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, cap, ji, jo, *ri, *ro, a.has_z); note_launch();
         RestRecs *tr = ri; ri = ro; ro = tr;
         int *tj = ji; ji = jo; jo = tj;
     }
-    k_rest_scatter<G><<<rb, 256, 0, s>>>(list, count, cap, a, *ri);
+    k_rest_scatter<G><<<rb, 256, 0, s>>>(list, count, cap, a, *ri); note_launch();
 }
 
 // Phase 2: R = number of nodes the walkers left (read back by the caller), scratch
@@ -456,7 +459,7 @@ void launch_node_attr(const TreeView &t, const AttrBufs &a, int attr, bool area,
                       cudaStream_t s)
 {
     int nb = grid_for(t.g.N, 256, sm);
-    k_node_attr<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, area, t.pixdim[0], t.pixdim[1], t.pixdim[2], out);
+    k_node_attr<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, area, t.pixdim[0], t.pixdim[1], t.pixdim[2], out); note_launch();
 }
 
 }  // namespace dcf

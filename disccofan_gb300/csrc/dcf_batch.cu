@@ -282,7 +282,7 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
     prof_begin(P_TILE, s);
 #define DCF_TB(T)                                                                                       \
     k_batch_tile_build<T><<<grid, TILE_THREADS, smem, s>>>((const T *)img, bg, imgs, tiles, ntiles, chunk, \
-                                                          next, gval, node, err)
+                                                          next, gval, node, err); note_launch()
     switch (dtype) {
     case U8: DCF_TB(uint8_t); break;
     case U16: DCF_TB(uint16_t); break;
@@ -297,10 +297,10 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
     if (seam.buckets > 0) {
         cudaMemsetAsync(seam.count, 0, 4, s);
         cudaMemsetAsync(seam.hist, 0, 4 * SEAM_BINS, s);
-        k_batch_seam_collect<<<grid_for(work, 256, sm), 256, 0, s>>>(node, bg, imgs, tiles, ntiles, seam);
+        k_batch_seam_collect<<<grid_for(work, 256, sm), 256, 0, s>>>(node, bg, imgs, tiles, ntiles, seam); note_launch();
         launch_seam_buckets(seam, node, bg.N, err, sm, s);
     } else {
-        k_batch_seam<<<grid_for(work, 128, sm), 128, 0, s>>>(node, bg, imgs, tiles, ntiles, err);
+        k_batch_seam<<<grid_for(work, 128, sm), 128, 0, s>>>(node, bg, imgs, tiles, ntiles, err); note_launch();
     }
     prof_end(P_SEAM, s);
     launch_canon(node, bg, parent, isroot, num_nodes, err, sm, s);
@@ -313,7 +313,7 @@ void launch_batch_attr_pixels(const Geom &bg, const BatchImg *imgs, const BatchT
     const long long work = (long long)ntiles * bg.tw * bg.th;
     const int nb = grid_for(work, 256, sm);
     prof_begin(P_ATTR_PIX, s);
-#define DCF_BP(G, E) k_batch_attr_pixels<G, E><<<nb, 256, 0, s>>>(gval, bg, imgs, tiles, ntiles, parent, isroot, a)
+#define DCF_BP(G, E) k_batch_attr_pixels<G, E><<<nb, 256, 0, s>>>(gval, bg, imgs, tiles, ntiles, parent, isroot, a); note_launch()
     switch (a.group * 2 + (a.exact_g ? 1 : 0)) {
     case 0: case 1: DCF_BP(0, false); break;
     case 2: case 3: DCF_BP(1, false); break;
@@ -340,6 +340,7 @@ void launch_batch_spectrum(const Geom &bg, const BatchImg *imgs, const BatchTile
     else
         k_batch_spectrum<false><<<grid, 256, 0, s>>>(bg, imgs, tiles, ntiles, parent, isroot, gval, a, a1, l1, n1, a2,
                                                      l2, n2, pixdim[0], pixdim[1], pixdim[2], spec);
+    note_launch();
     prof_end(P_SPECTRUM, s);
 }
 

@@ -261,10 +261,13 @@ __global__ void k_seam_bucket(SeamEdges e, int b, unsigned long long *gnode, lon
 
 void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, unsigned *err, int sm, cudaStream_t s)
 {
-    k_seam_bounds<<<1, 1024, 0, s>>>(e);
-    k_seam_scatter<<<grid_for(e.cap, 256, sm), 256, 0, s>>>(e);
+    k_seam_bounds<<<1, 1024, 0, s>>>(e); note_launch();
+    k_seam_scatter<<<grid_for(e.cap, 256, sm), 256, 0, s>>>(e); note_launch();
     const int gb = grid_for(e.cap / e.buckets + 1, 128, sm);
-    for (int b = 0; b < e.buckets; b++) k_seam_bucket<<<gb, 128, 0, s>>>(e, b, node, n, err);
+    for (int b = 0; b < e.buckets; b++) {
+        k_seam_bucket<<<gb, 128, 0, s>>>(e, b, node, n, err);
+        note_launch();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -300,7 +303,7 @@ void launch_canon(unsigned long long *node, const Geom &g, int *parent, unsigned
                   unsigned long long *num_nodes, unsigned *err, int sm_count, cudaStream_t s)
 {
     prof_begin(P_CANON, s);
-    k_canon<<<grid_for(g.N, 256, sm_count), 256, 0, s>>>(node, g, parent, isroot, num_nodes, err);
+    k_canon<<<grid_for(g.N, 256, sm_count), 256, 0, s>>>(node, g, parent, isroot, num_nodes, err); note_launch();
     prof_end(P_CANON, s);
 }
 
@@ -312,7 +315,7 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
     dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
     const size_t smem = tile_smem_bytes(TW, TH, TD);
     prof_begin(P_TILE, s);
-    k_tile_build<T, MIN><<<grid, TILE_THREADS, smem, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err);
+    k_tile_build<T, MIN><<<grid, TILE_THREADS, smem, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err); note_launch();
     prof_end(P_TILE, s);
     prof_begin(P_SEAM, s);
     {
@@ -321,10 +324,10 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
             SeamEdges e = a.seam;
             cudaMemsetAsync(e.count, 0, 4, s);
             cudaMemsetAsync(e.hist, 0, 4 * SEAM_BINS, s);
-            k_seam_collect<<<grid_for(work, 256, a.sm_count), 256, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, e);
+            k_seam_collect<<<grid_for(work, 256, a.sm_count), 256, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, e); note_launch();
             launch_seam_buckets(e, a.node, a.g.N, a.err, a.sm_count, s);
         } else {
-            k_seam_direct<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err);
+            k_seam_direct<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err); note_launch();
         }
     }
     prof_end(P_SEAM, s);
@@ -337,10 +340,10 @@ void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsig
     int nb = grid_for(n, 256, sm_count);
     prof_begin(P_STATS, s);
     switch (dtype) {
-    case U8: k_stats<uint8_t><<<nb, 256, 0, s>>>((const uint8_t *)img, n, kmin, kmax, nans); break;
-    case U16: k_stats<uint16_t><<<nb, 256, 0, s>>>((const uint16_t *)img, n, kmin, kmax, nans); break;
-    case U32: k_stats<uint32_t><<<nb, 256, 0, s>>>((const uint32_t *)img, n, kmin, kmax, nans); break;
-    default: k_stats<float><<<nb, 256, 0, s>>>((const float *)img, n, kmin, kmax, nans); break;
+    case U8: k_stats<uint8_t><<<nb, 256, 0, s>>>((const uint8_t *)img, n, kmin, kmax, nans); note_launch(); break;
+    case U16: k_stats<uint16_t><<<nb, 256, 0, s>>>((const uint16_t *)img, n, kmin, kmax, nans); note_launch(); break;
+    case U32: k_stats<uint32_t><<<nb, 256, 0, s>>>((const uint32_t *)img, n, kmin, kmax, nans); note_launch(); break;
+    default: k_stats<float><<<nb, 256, 0, s>>>((const float *)img, n, kmin, kmax, nans); note_launch(); break;
     }
     prof_end(P_STATS, s);
 }

@@ -13,6 +13,9 @@ enum ProfId : int {
 };
 void prof_begin(int id, cudaStream_t s);
 void prof_end(int id, cudaStream_t s);
+// counts one kernel launch for the context whose API call is running on this thread
+// (dcf_ctx_launch_count); every launch site calls it right after the launch
+void note_launch();
 
 constexpr int TILE_THREADS = 256;
 constexpr int TILE_MAX_PIX = 4096;             // largest build tile (16-bit local indices)

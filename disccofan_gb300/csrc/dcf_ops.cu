@@ -240,16 +240,16 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
     k_flag<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
-                              w.target);
+                              w.target); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
     const double *accp = nullptr;
     if (rule == 0) {
-        k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err);
+        k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err); note_launch();
     } else if (rule == 2) {
         cudaMemsetAsync(w.kept, 0, t.g.N * sizeof(unsigned), s);
-        k_mark_kept<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.kept, err);
-        k_resolve<unsigned><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.kept, w.target, err);
+        k_mark_kept<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.kept, err); note_launch();
+        k_resolve<unsigned><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.kept, w.target, err); note_launch();
     } else {
         const int R = rounds_for(depth_bound);
         int *j0 = w.jump, *j1 = w.jump2;
@@ -260,7 +260,7 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
             cudaMemsetAsync(known, 0, t.g.N, s);
             for (long long launch = 0; launch <= t.g.N / SUB_STACK + 1; launch++) {
                 cudaMemsetAsync(w.remaining, 0, sizeof(unsigned), s);
-                k_sub_exact<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, val, known, w.remaining);
+                k_sub_exact<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, val, known, w.remaining); note_launch();
                 unsigned left = 0;
                 cudaMemcpyAsync(&left, w.remaining, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
                 cudaStreamSynchronize(s);
@@ -270,18 +270,18 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
             rule = 4;
         } else if (rule == 3) {
             double *a0 = w.acc, *a1 = w.acc2;
-            k_sub_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, j0, a0);
+            k_sub_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, j0, a0); note_launch();
             for (int r = 0; r < R; r++) {
-                k_jump_sum<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, a0, j1, a1);
+                k_jump_sum<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, a0, j1, a1); note_launch();
                 int *tj = j0; j0 = j1; j1 = tj;
                 double *ta = a0; a0 = a1; a1 = ta;
             }
             accp = a0;
         } else {
             int *b0 = w.target, *b1 = w.best2;
-            k_min_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, j0, b0);
+            k_min_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, j0, b0); note_launch();
             for (int r = 0; r < R; r++) {
-                k_jump_last<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, b0, j1, b1);
+                k_jump_last<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, b0, j1, b1); note_launch();
                 int *tj = j0; j0 = j1; j1 = tj;
                 int *tb = b0; b0 = b1; b1 = tb;
             }
@@ -291,7 +291,7 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     prof_end(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
     prof_begin(P_FILTER_OUT, s);
 #define DCF_OUT(R) \
-    k_filter_out<R><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, w.target, accp, extract, t.tree_min, t.kmax, out)
+    k_filter_out<R><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, w.target, accp, extract, t.tree_min, t.kmax, out); note_launch()
     switch (rule) {
     case 0: DCF_OUT(0); break;
     case 1: DCF_OUT(1); break;
@@ -318,7 +318,7 @@ void launch_check(const TreeView &t, const AttrBufs &a, int attr, float *out, in
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_CHECK, s);
-    k_check<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, a, attr, t.pixdim[0], t.pixdim[1], t.pixdim[2], out);
+    k_check<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, a, attr, t.pixdim[0], t.pixdim[1], t.pixdim[2], out); note_launch();
     prof_end(P_CHECK, s);
 }
 
@@ -375,7 +375,7 @@ void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_SPECTRUM, s);
     k_spectrum<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
-                                  t.pixdim[1], t.pixdim[2], spec);
+                                  t.pixdim[1], t.pixdim[2], spec); note_launch();
     prof_end(P_SPECTRUM, s);
 }
 
@@ -431,8 +431,8 @@ void launch_adjoint(const TreeView &t, const AttrBufs &a, const AdjointArgs &j, 
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_ADJOINT, s);
-    k_adjoint<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, a, j, t.pixdim[0], t.pixdim[1], t.pixdim[2]);
-    k_adjoint_out<<<nb, 256, 0, s>>>(t.g.N, j.acc, j.grad);
+    k_adjoint<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, a, j, t.pixdim[0], t.pixdim[1], t.pixdim[2]); note_launch();
+    k_adjoint_out<<<nb, 256, 0, s>>>(t.g.N, j.acc, j.grad); note_launch();
     prof_end(P_ADJOINT, s);
 }
 
@@ -443,10 +443,10 @@ void launch_direct_targets(const TreeView &t, const AttrBufs &a, int attr, doubl
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
     k_flag<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
-                              w.target);
+                              w.target); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(P_RESOLVE, s);
-    k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err);
+    k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err); note_launch();
     prof_end(P_RESOLVE, s);
 }
 
