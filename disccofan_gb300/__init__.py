@@ -111,6 +111,8 @@ def library() -> C.CDLL:
         "dcf_pattern_spectrum": [vp, vp, i, vp, i, vp, i],
         "dcf_pattern_spectrum2d": [vp, vp, i, vp, i, i, vp, i, vp, i],
         "dcf_lvec_read": [C.c_char_p, d, vp, i, C.POINTER(i)],
+        "dcf_tree_export": [vp, vp, i, C.c_char_p],
+        "dcf_fits_read": [C.c_char_p, vp, u64, C.POINTER(u64 * 3), C.POINTER(i)],
         "dcf_batch_create": [vp, i, vp, vp, i, i, i, vp, C.POINTER(vp)],
         "dcf_batch_destroy": [vp],
         "dcf_batch_info": [vp, C.POINTER(u64), C.POINTER(u64), vp, C.POINTER(u64)],
@@ -168,6 +170,23 @@ def read_lvec(path: str, imscale: float = 1.0) -> np.ndarray:
     if st:
         raise DcfError(st, path)
     return out
+
+
+def read_fits(path: str) -> np.ndarray:
+    """Primary FITS image as the reference reads it (float32, BZERO + BSCALE * raw),
+    shaped (H, W) or (D, H, W)."""
+    L = library()
+    dims = (C.c_uint64 * 3)()
+    bp = C.c_int()
+    st = L.dcf_fits_read(path.encode(), None, 0, C.byref(dims), C.byref(bp))
+    if st:
+        raise DcfError(st, path)
+    w, h, d = dims[0], dims[1], dims[2]
+    out = np.empty(w * h * d, np.float32)
+    st = L.dcf_fits_read(path.encode(), out.ctypes.data, out.size, C.byref(dims), C.byref(bp))
+    if st:
+        raise DcfError(st, path)
+    return out.reshape((h, w) if d == 1 else (d, h, w))
 
 
 class Context:
@@ -306,6 +325,12 @@ class Tree:
         # area (0) is readable from every group's records
         if attribute != 0 and ATTR_GROUP[attribute] != ATTR_GROUP[self.attribute]:
             self.set_attribute(attribute)
+
+    def export(self, path: str, attribute: int | None = None):
+        """Write the tree file (write_tree's format) for an attribute of the current group."""
+        a = self.attribute if attribute is None else attribute
+        self._ensure_group(a)
+        self.ctx.check(self.ctx.lib.dcf_tree_export(self.ctx.h, self.h, a, path.encode()), "tree_export")
 
     def info(self):
         n, m, c, g = C.c_uint64(), C.c_uint64(), C.c_int(), C.c_float()

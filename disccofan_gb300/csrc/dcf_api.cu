@@ -701,6 +701,76 @@ dcf_status dcf_node_attribute(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int area,
     return check_nan(ctx, t, nullptr);
 }
 
+// readout of attribute (or tree-file column) `code` into host memory
+static dcf_status readout_host(dcf_ctx *ctx, dcf_tree *t, int code, bool area, std::vector<double> &out)
+{
+    const size_t N = (size_t)t->g.N;
+    void *s;
+    dcf_status st = scratch(ctx, 0, N * 8, &s);
+    if (st != DCF_OK) return st;
+    launch_node_attr(view_of(t), t->attr, code, area, (double *)s, ctx->sm_count, ctx->stream);
+    if ((st = check_launch(ctx, 1)) != DCF_OK) return st;
+    out.resize(N);
+    CU(cudaMemcpyAsync(out.data(), s, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+dcf_status dcf_tree_export(dcf_ctx *ctx, dcf_tree *t, int attr_idx, const char *path)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !t || !path) return DCF_ERR_INVALID;
+    if (attr_idx < 0 || attr_idx >= DCF_NUM_ATTRIBUTES) return set_err(ctx, DCF_ERR_INVALID, "bad attribute %d", attr_idx);
+    if (!t->attr_mem || ATTR_GROUP[attr_idx] != t->attr.group)
+        return set_err(ctx, DCF_ERR_STATE, "attribute %d is not in the tree's group (use dcf_tree_set_attribute)",
+                       attr_idx);
+    const int group = ATTR_GROUP[attr_idx];
+    const size_t N = (size_t)t->g.N;
+    std::vector<int64_t> par(N);
+    std::vector<float> gv(N);
+    dcf_status st;
+    if ((st = dcf_tree_parent(ctx, t, par.data(), 0)) != DCF_OK) return st;
+    if ((st = dcf_tree_gval(ctx, t, gv.data(), 0)) != DCF_OK) return st;
+    std::vector<double> area;
+    if ((st = readout_host(ctx, t, attr_idx, true, area)) != DCF_OK) return st;
+    // the group's extra columns (io.c:1454-1462 header, :1518-1547 rows)
+    static const int g1[] = {1, 2, 3, 4, 5}, g2[] = {6, 7, 8}, g3[] = {9, 10, 11},
+                     g4[] = {INERTIA_COL0, INERTIA_COL0 + 1, INERTIA_COL0 + 2, INERTIA_COL0 + 3, INERTIA_COL0 + 4,
+                             INERTIA_COL0 + 5, 14, 15, 16, 17};
+    const int *codes = group == 1 ? g1 : group == 2 ? g2 : group == 3 ? g3 : g4;
+    const int ncol = group == 0 ? 0 : group == 1 ? 5 : (group == 4 ? 10 : 3);
+    std::vector<std::vector<double>> cols(ncol);
+    for (int c = 0; c < ncol; c++)
+        if ((st = readout_host(ctx, t, codes[c], false, cols[c])) != DCF_OK) return st;
+    FILE *f = fopen(path, "w");
+    if (!f) return set_err(ctx, DCF_ERR_IO, "cannot open %s for writing", path);
+    fprintf(f, "index,x,y,z,gval,parent,flux,area,");
+    if (group == 1) fprintf(f, "area_enc_rect,diag_enc_rect,x_extent,y_extent,z_extent");
+    else if (group == 2) fprintf(f, "x_mean,y_mean,z_mean");
+    else if (group == 3) fprintf(f, "x_wmean,y_wmean,z_wmean");
+    else if (group == 4) fprintf(f, "x_mean,y_mean,z_mean,x_wmean,y_wmean,z_wmean,elong,flat,spars,ncomp");
+    fprintf(f, "\n");
+    const uint64_t W = (uint64_t)t->g.W, WH = (uint64_t)t->g.WH;
+    for (size_t i = 0; i < N; i++) {
+        const int64_t q = par[i];
+        if (q >= 0 && gv[q] == gv[i]) continue;  // not a level root (flood.h:29-32)
+        const long x = (long)((i % WH) % W), y = (long)((i % WH) / W), z = (long)(i / WH);
+        const long size = (long)area[i];
+        const float dh = q >= 0 ? gv[i] - gv[q] : gv[i];
+        fprintf(f, "%ld,%ld,%ld,%ld,%f,%ld,%f,%ld,", (long)i, x, y, z, (double)gv[i], (long)q,
+                (double)(dh * (float)size), size);
+        if (group == 1 || group == 2 || group == 3) {
+            for (int c = 0; c < ncol; c++) fprintf(f, c ? ",%.2f" : "%.2f", (double)(float)cols[c][i]);
+        } else if (group == 4) {
+            for (int c = 0; c < 6; c++) fprintf(f, "%.2f,", (double)(float)cols[c][i]);
+            fprintf(f, "%.3f,%.3f,%.3f,%.4f ", (double)(float)cols[6][i], (double)(float)cols[7][i],
+                    (double)(float)cols[8][i], (double)(float)cols[9][i]);
+        }
+        fprintf(f, "\n");
+    }
+    if (fclose(f) != 0) return set_err(ctx, DCF_ERR_IO, "write to %s failed", path);
+    return DCF_OK;
+}
+
 // longest possible root path: every node on it has a distinct grey level
 static long long depth_bound(const dcf_tree *t)
 {

@@ -450,7 +450,9 @@ __global__ void k_node_attr(Geom g, const unsigned char *__restrict__ isroot, At
     const float pd[3] = {pd0, pd1, pd2};
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
          p += (long long)gridDim.x * blockDim.x) {
-        out[p] = isroot[p] ? (area ? area_value(a, (int)p, pd) : attr_value(a, attr, (int)p, pd))
+        out[p] = isroot[p] ? (area ? area_value(a, (int)p, pd)
+                                   : attr >= INERTIA_COL0 ? inertia_column(a, attr - INERTIA_COL0, (int)p, pd)
+                                                          : attr_value(a, attr, (int)p, pd))
                            : __longlong_as_double(0x7ff8000000000000LL);
     }
 }

@@ -106,6 +106,17 @@ __device__ __forceinline__ void inertia_arr(const AttrBufs &a, int u, const floa
     in[14] = (double)pd[2] * gsum(a, 4, u);
 }
 
+// Centroids as the inertia group reports them in the tree file
+// (inertia_attribute_arr, attributes.c:629-641): k = 0..2 mean x, y, z =
+// in[1+k] / in[0]; k = 3..5 grey-weighted means in[12+k-3] / in[10].  They differ
+// from the mean and weighted-mean attributes (6-11) when the pixel size is not 1.
+__device__ __forceinline__ double inertia_column(const AttrBufs &a, int k, int u, const float *pd)
+{
+    double in[15];
+    inertia_arr(a, u, pd, in);
+    return k < 3 ? in[1 + k] / in[0] : in[12 + k - 3] / in[10];
+}
+
 __device__ __forceinline__ double attr_value(const AttrBufs &a, int attr, int u, const float *pd)
 {
     switch (attr) {

@@ -161,7 +161,10 @@ void launch_batch_attr_pixels(const Geom &bg, const BatchImg *imgs, const BatchT
                               const float *gval, const int *parent, const unsigned char *isroot, AttrBufs &a,
                               int sm_count, cudaStream_t s);
 
-// attribute readout of every level root into a double array (NaN elsewhere)
+// attribute readout of every level root into a double array (NaN elsewhere);
+// attr >= INERTIA_COL0 (INERTIA_COL0 + k): the inertia group's tree-file centroid
+// column k (inertia_column)
+constexpr int INERTIA_COL0 = 100;
 void launch_node_attr(const TreeView &t, const AttrBufs &a, int attr, bool area, double *out, int sm_count,
                       cudaStream_t s);
 

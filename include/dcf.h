@@ -26,6 +26,8 @@
  *                                                             src/sources/operation.c:88-100
  *   dcf_dmp                   perform_dmp_operation           src/sources/operation.c:63
  *   dcf_lvec_read             lambda_vector_read              src/sources/lambdavec.c:35
+ *   dcf_tree_export           write_tree                      src/sources/io.c:1431
+ *   dcf_fits_read             the FITS branch of the tile reader src/sources/io.c:624-706
  *   dcf_batch_*               (no reference counterpart: many cutouts per launch)
  *   dcf_adjoint_*             (no reference counterpart: gradients for float images)
  */
@@ -216,6 +218,19 @@ dcf_status dcf_batch_adjoint(dcf_ctx *ctx, dcf_batch *batch, const float *grad_f
 /* The same adjoint for one tree (a float32 max-tree) and the operations in ops. */
 dcf_status dcf_tree_adjoint(dcf_ctx *ctx, dcf_tree *tree, const dcf_op_set *ops, const float *grad_filtered,
                             const double *grad_spectrum, float *grad_pixels, int on_device);
+
+/* ---- files ---- */
+/* Write the tree in the reference's tree-file format (write_tree, io.c:1431-1573,
+ * one rank, no borders): a header, then one line per level root in index order
+ * with index, x, y, z, gval, parent, flux = dh*area, area and the columns of
+ * attr_idx's group.  attr_idx must be in the tree's current group. */
+dcf_status dcf_tree_export(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, const char *path);
+/* Read the primary image of a FITS file as the reference's FITS input does
+ * (io.c:624-706, CFITSIO fits_read_pix into float): every pixel BZERO + BSCALE*raw
+ * as float, x fastest.  BITPIX 8/16/32/-32/-64, NAXIS 1-3.  dims receives the
+ * axis lengths (1 for missing axes), *bitpix the file's BITPIX; out == NULL reads
+ * the header only; capacity (in pixels) must cover dims[0]*dims[1]*dims[2]. */
+dcf_status dcf_fits_read(const char *path, float *out, uint64_t capacity, uint64_t dims[3], int *bitpix);
 
 /* ---- lambda vectors ---- */
 /* Read a "#LambdaVector file..." file: out[0] = 0, out[i] = value_i / imscale.

@@ -17,6 +17,7 @@ Usage:  python tests/golden/make_golden.py [/path/to/reference]
 """
 from __future__ import annotations
 
+import hashlib
 import os
 import struct
 import sys
@@ -178,6 +179,10 @@ def main(refdir: str = "/root/reference") -> None:
     chk_ncomp = read_fits(os.path.join(ck, "GT_2D_check_ncomp.fits")).astype(np.float32)
     lena_fits = read_fits(os.path.join(ck, "lena512.fits")).astype(np.uint8)
     assert np.array_equal(lena_fits, lena), "input_image.png (flipped) != lena512.fits"
+    # trailing newlines normalised to one (the fixture ends with an extra blank line
+    # that write_tree itself does not print)
+    tree_bytes = open(os.path.join(ck, "GT_tree.txt"), "rb").read().rstrip(b"\n") + b"\n"
+    tree_lines = tree_bytes.split(b"\n")
     idx, par, area = [], [], []
     with open(os.path.join(ck, "GT_tree.txt")) as f:
         next(f)
@@ -193,7 +198,12 @@ def main(refdir: str = "/root/reference") -> None:
         lena=lena, gt_area_200=gt_area, gt_ncomp_0_2=gt_ncomp,
         check_area_c4=chk_area, check_area_c8=chk_area8, check_ncomp_c4=chk_ncomp,
         tree_index=np.array(idx, np.int64), tree_parent=np.array(par, np.int64),
-        tree_area=np.array(area, np.int64))
+        tree_area=np.array(area, np.int64),
+        # the whole tree file, for the end-to-end check of the tree export: its
+        # SHA-256, length and a few lines (header, first rows, last rows)
+        tree_txt_sha256=np.frombuffer(hashlib.sha256(tree_bytes).digest(), np.uint8),
+        tree_txt_bytes=np.int64(len(tree_bytes)),
+        tree_txt_sample=np.array([l.decode() for l in tree_lines[:4] + tree_lines[-3:-1]]))
 
     oracle.build(ref=True)
     ref = oracle.Reference()

@@ -51,6 +51,23 @@ def test_lena_checks_match_reference_fixtures(ctx, lena):
     assert np.array_equal(t8.check(0), lena["check_area_c8"])
 
 
+def test_tree_export_matches_reference_tree_file(ctx, lena, tmp_path):
+    # end to end: the tree file written from the GPU tree is byte-identical to the
+    # reference's GT_tree.txt (inertia group, 4-connectivity), compared through its
+    # SHA-256 with a few lines for diagnosis
+    import hashlib
+    t = gpu_tree(ctx, lena["lena"], 4, "max", 17)
+    path = tmp_path / "tree.txt"
+    t.export(str(path), 17)
+    data = path.read_bytes()
+    lines = data.decode().split("\n")
+    sample = [str(x) for x in lena["tree_txt_sample"]]
+    assert lines[:4] == sample[:4]
+    assert lines[-3:-1] == sample[-2:]
+    assert len(data) == int(lena["tree_txt_bytes"])
+    assert hashlib.sha256(data).digest() == bytes(lena["tree_txt_sha256"])
+
+
 def test_lena_tree_matches_reference_tree_file(ctx, lena):
     t = gpu_tree(ctx, lena["lena"], 4)
     par = t.parent()
