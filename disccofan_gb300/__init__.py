@@ -112,6 +112,7 @@ def library() -> C.CDLL:
         "dcf_pattern_spectrum2d": [vp, vp, i, vp, i, i, vp, i, vp, i],
         "dcf_lvec_read": [C.c_char_p, d, vp, i, C.POINTER(i)],
         "dcf_tree_export": [vp, vp, i, C.c_char_p],
+        "dcf_csl": [vp, vp, i, vp, i, vp, vp, vp, i],
         "dcf_fits_read": [C.c_char_p, vp, u64, C.POINTER(u64 * 3), C.POINTER(i)],
         "dcf_batch_create": [vp, i, vp, vp, i, i, i, vp, C.POINTER(vp)],
         "dcf_batch_destroy": [vp],
@@ -325,6 +326,16 @@ class Tree:
         # area (0) is readable from every group's records
         if attribute != 0 and ATTR_GROUP[attribute] != ATTR_GROUP[self.attribute]:
             self.set_attribute(attribute)
+
+    def csl(self, attribute: int, lvec):
+        """CSL segmentation (perform_csl): (contrast, scale, luminance) images;
+        lvec includes the leading 0 (read_lvec / lvec_from_values)."""
+        self._ensure_group(attribute)
+        lv = np.ascontiguousarray(lvec, np.float32)
+        outs = [np.empty(self.n, np.float32) for _ in range(3)]
+        self.ctx.check(self.ctx.lib.dcf_csl(self.ctx.h, self.h, attribute, lv.ctypes.data, lv.size,
+                                            *[o.ctypes.data for o in outs], 0), "csl")
+        return tuple(self._shape(o) for o in outs)
 
     def export(self, path: str, attribute: int | None = None):
         """Write the tree file (write_tree's format) for an attribute of the current group."""

@@ -701,6 +701,37 @@ dcf_status dcf_node_attribute(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int area,
     return check_nan(ctx, t, nullptr);
 }
 
+dcf_status dcf_csl(dcf_ctx *ctx, dcf_tree *t, int attr_idx, const float *lvec, int num_lambdas, float *contrast,
+                   float *scale, float *luminance, int on_device)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !t || !lvec || num_lambdas < 1 || !contrast || !scale || !luminance) return DCF_ERR_INVALID;
+    dcf_status st = check_attr(ctx, t, attr_idx);
+    if (st != DCF_OK) return st;
+    const size_t N = (size_t)t->g.N;
+    const size_t lbytes = ((size_t)num_lambdas * 4 + 255) / 256 * 256;
+    void *work, *io;
+    if ((st = scratch(ctx, 13, csl_work_bytes((long long)N) + lbytes, &work)) != DCF_OK) return st;
+    float *dl = (float *)((char *)work + csl_work_bytes((long long)N));
+    CU(cudaMemcpyAsync(dl, lvec, (size_t)num_lambdas * 4, cudaMemcpyHostToDevice, ctx->stream));
+    float *out[3] = {contrast, scale, luminance};
+    if (!on_device) {
+        if ((st = scratch(ctx, 7, N * 12, &io)) != DCF_OK) return st;
+        for (int i = 0; i < 3; i++) out[i] = (float *)io + i * N;
+    }
+    launch_csl(view_of(t), t->attr, attr_idx, dl, num_lambdas, out[0], out[1], out[2], work, ctx->d_err + 1,
+               ctx->sm_count, ctx->stream);
+    if ((st = check_launch(ctx, 0)) != DCF_OK) return st;
+    if (!on_device) {
+        CU(cudaMemcpyAsync(contrast, out[0], N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaMemcpyAsync(scale, out[1], N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaMemcpyAsync(luminance, out[2], N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    st = sync_and_check(ctx);
+    if (st != DCF_OK) return st;
+    return check_nan(ctx, t, nullptr);
+}
+
 // readout of attribute (or tree-file column) `code` into host memory
 static dcf_status readout_host(dcf_ctx *ctx, dcf_tree *t, int code, bool area, std::vector<double> &out)
 {

@@ -188,6 +188,12 @@ void launch_check(const TreeView &t, const AttrBufs &a, int attr, float *out, in
 void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *l1, int n1, int a2,
                      const float *l2, int n2, double *spec, int sm_count, cudaStream_t s);
 void launch_level_out(const TreeView &t, float *out, int sm_count, cudaStream_t s);
+// CSL segmentation (csl.c:27-124) into three per-pixel float images; lv: n lambdas
+// (device, with the leading 0); work: csl_work_bytes(N) bytes; synchronises the
+// stream between its rounds
+size_t csl_work_bytes(long long n);
+void launch_csl(const TreeView &t, const AttrBufs &a, int attr, const float *lv, int n, float *contrast, float *scale,
+                float *luminance, void *work, unsigned *remaining, int sm_count, cudaStream_t s);
 // per-cutout 2-D spectra of a batch, spec[img*n1*n2 + s1 + s2*n1] (accumulated)
 void launch_batch_spectrum(const Geom &bg, const BatchImg *imgs, const BatchTile *tiles, int ntiles, const int *parent,
                            const unsigned char *isroot, const float *gval, const AttrBufs &a, int a1, const float *l1,

@@ -380,6 +380,165 @@ void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *
 }
 
 // ---------------------------------------------------------------------------
+// CSL segmentation (node_differential_seg, csl.c:27-124): for every node, along its
+// root path, the largest run of contrast (summed dh) within one scale class, the
+// scale class it was found in and the grey level where it peaked.  State of a
+// level root u: maxScale, maxDH, maxOrig, curScale, curDH.  A node whose scale is
+// past the last lambda, or the root, restarts the state; any other node extends its
+// parent's state with dh(u).  Evaluated like the exact subtractive rule: each node
+// walks up (at most CSL_STACK steps) to a node whose state is known or that
+// restarts, then evaluates the walked path downward; the rest retry next launch.
+// ---------------------------------------------------------------------------
+constexpr int CSL_STACK = 48;
+
+// find_scale_csl (csl.c:9-25): past the last lambda -> n (one beyond the bins)
+__device__ __forceinline__ int find_scale_csl(const float *lv, int n, double v)
+{
+    int upper = n - 1, lower = 0;
+    if (v >= (double)lv[upper]) return upper + 1;
+    int mid = (upper + lower) / 2;
+    while (mid != lower) {
+        if (v >= (double)lv[mid]) lower = mid;
+        else upper = mid;
+        mid = (upper + lower) / 2;
+    }
+    return lower;
+}
+
+struct CslState {
+    int *max_scale, *cur_scale, *my_scale;
+    float *max_dh, *max_orig, *cur_dh;
+    unsigned char *known;
+};
+
+__global__ void k_csl_init(Geom g, const unsigned char *__restrict__ isroot, AttrBufs a, int attr,
+                           const float *__restrict__ lv, int n, float pd0, float pd1, float pd2, CslState c)
+{
+    const float pd[3] = {pd0, pd1, pd2};
+    GRID_LOOP(p, g.N)
+    {
+        c.known[p] = 0;
+        if (isroot[p]) c.my_scale[p] = find_scale_csl(lv, n, attr_value(a, attr, (int)p, pd));
+    }
+}
+
+__global__ void k_csl(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+                      const float *__restrict__ gval, int n, CslState c, unsigned *remaining)
+{
+    unsigned left = 0;
+    GRID_LOOP(p, g.N)
+    {
+        if (!isroot[p] || ((volatile unsigned char *)c.known)[p]) continue;
+        int stk[CSL_STACK];
+        int depth = 0, v = (int)p;
+        bool have = false, restart = false;
+        while (depth < CSL_STACK) {
+            if (((volatile unsigned char *)c.known)[v]) { have = true; break; }
+            stk[depth++] = v;
+            if (parent[v] == NONE || c.my_scale[v] == n) { restart = true; break; }
+            v = parent[v];
+        }
+        if (!have && !restart) { left++; continue; }
+        __threadfence();  // pairs with the writer's fence between state and flag
+        int ms, cs;
+        float mdh, mo, cdh;
+        int j = depth - 1;
+        if (restart) {  // stk[j] starts a state of its own
+            const int r = stk[j];
+            const bool root = parent[r] == NONE;
+            ms = root ? c.my_scale[r] : n;
+            mo = root ? gval[r] : 0.0f;
+            mdh = 0.0f;
+            cdh = 0.0f;
+            cs = ms;
+        } else {
+            ms = ((volatile int *)c.max_scale)[v];
+            cs = ((volatile int *)c.cur_scale)[v];
+            mdh = ((volatile float *)c.max_dh)[v];
+            mo = ((volatile float *)c.max_orig)[v];
+            cdh = ((volatile float *)c.cur_dh)[v];
+            j = depth;  // every stacked node extends a known state
+        }
+        for (int k = restart ? j : j - 1; k >= 0; k--) {
+            const int w = stk[k];
+            if (!(restart && k == j)) {
+                const int sw = c.my_scale[w];
+                const float dh = __fsub_rn(gval[w], gval[parent[w]]);
+                if (sw == cs) cdh = __fadd_rn(cdh, dh);
+                else {
+                    cdh = dh;
+                    cs = sw;
+                }
+                if (cdh >= mdh) {
+                    mdh = cdh;
+                    ms = cs;
+                    mo = gval[w];
+                }
+            }
+            ((volatile int *)c.max_scale)[w] = ms;
+            ((volatile int *)c.cur_scale)[w] = cs;
+            ((volatile float *)c.max_dh)[w] = mdh;
+            ((volatile float *)c.max_orig)[w] = mo;
+            ((volatile float *)c.cur_dh)[w] = cdh;
+            __threadfence();
+            ((volatile unsigned char *)c.known)[w] = 1;
+        }
+    }
+    for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
+    if ((threadIdx.x & 31) == 0 && left) atomicAdd(remaining, left);
+}
+
+__global__ void k_csl_out(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent, CslState c,
+                          float *contrast, float *scale, float *luminance)
+{
+    GRID_LOOP(p, g.N)
+    {
+        const int u = isroot[p] ? (int)p : parent[p];
+        contrast[p] = c.max_dh[u];
+        scale[p] = (float)c.max_scale[u];
+        luminance[p] = c.max_orig[u];
+    }
+}
+
+// the seven arrays launch_csl carves, each rounded up to 256 bytes (so that what a
+// caller places after them stays 256-byte aligned)
+size_t csl_work_bytes(long long n)
+{
+    const size_t a4 = ((size_t)n * 4 + 255) / 256 * 256, a1 = ((size_t)n + 255) / 256 * 256;
+    return 6 * a4 + a1;
+}
+
+void launch_csl(const TreeView &t, const AttrBufs &a, int attr, const float *lv, int n, float *contrast, float *scale,
+                float *luminance, void *work, unsigned *remaining, int sm, cudaStream_t s)
+{
+    const long long N = t.g.N;
+    char *m = (char *)work;
+    auto take = [&](size_t b) { void *p = m; m += (b + 255) / 256 * 256; return p; };
+    CslState c;
+    c.max_scale = (int *)take(4 * N);
+    c.cur_scale = (int *)take(4 * N);
+    c.my_scale = (int *)take(4 * N);
+    c.max_dh = (float *)take(4 * N);
+    c.max_orig = (float *)take(4 * N);
+    c.cur_dh = (float *)take(4 * N);
+    c.known = (unsigned char *)take(N);
+    const int nb = grid_for(N, 256, sm);
+    k_csl_init<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lv, n, t.pixdim[0], t.pixdim[1], t.pixdim[2], c);
+    note_launch();
+    for (long long launch = 0; launch <= N / CSL_STACK + 1; launch++) {
+        cudaMemsetAsync(remaining, 0, sizeof(unsigned), s);
+        k_csl<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, n, c, remaining);
+        note_launch();
+        unsigned left = 0;
+        cudaMemcpyAsync(&left, remaining, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        if (left == 0) break;
+    }
+    k_csl_out<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, c, contrast, scale, luminance);
+    note_launch();
+}
+
+// ---------------------------------------------------------------------------
 // adjoint (no reference counterpart)
 // ---------------------------------------------------------------------------
 // With the tree fixed, the direct-rule output out(p) = level(target(node(p))) and

@@ -25,6 +25,8 @@
  *                             perform_pattern_spectrum)       src/sources/pattern.c:110,
  *                                                             src/sources/operation.c:88-100
  *   dcf_dmp                   perform_dmp_operation           src/sources/operation.c:63
+ *   dcf_csl                   perform_csl / tree_differential src/sources/operation.c:31,
+ *                                                             src/sources/csl.c:27-146
  *   dcf_lvec_read             lambda_vector_read              src/sources/lambdavec.c:35
  *   dcf_tree_export           write_tree                      src/sources/io.c:1431
  *   dcf_fits_read             the FITS branch of the tile reader src/sources/io.c:624-706
@@ -218,6 +220,15 @@ dcf_status dcf_batch_adjoint(dcf_ctx *ctx, dcf_batch *batch, const float *grad_f
 /* The same adjoint for one tree (a float32 max-tree) and the operations in ops. */
 dcf_status dcf_tree_adjoint(dcf_ctx *ctx, dcf_tree *tree, const dcf_op_set *ops, const float *grad_filtered,
                             const double *grad_spectrum, float *grad_pixels, int on_device);
+
+/* CSL segmentation (perform_csl operation.c:31, node_differential_seg
+ * csl.c:27-124; the reference implements only this first part): per pixel, along
+ * its node's root path, the largest contrast (dh summed within one scale class of
+ * attr_idx on the lambda bins lvec, num_lambdas values with the leading 0), the
+ * scale class it was found in and the grey level where it peaked.  Three
+ * width*height*depth float images. */
+dcf_status dcf_csl(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, const float *lvec, int num_lambdas, float *contrast,
+                   float *scale, float *luminance, int on_device);
 
 /* ---- files ---- */
 /* Write the tree in the reference's tree-file format (write_tree, io.c:1431-1573,

@@ -152,6 +152,16 @@ class Reference:
             os.unlink(p2)
         return out.reshape(n2, n1)
 
+    def csl(self, attr: int, lvec, imscale: float = 1.0):
+        """perform_csl (operation.c:31): (contrast, scale, luminance) images."""
+        p = write_lvec(lvec)
+        try:
+            out = np.empty(3 * self.n, np.float32)
+            self._op("csl", attr, 0, 0, 0.0, p, imscale, out=out)
+        finally:
+            os.unlink(p)
+        return out[:self.n].copy(), out[self.n:2 * self.n].copy(), out[2 * self.n:].copy()
+
     def parent(self) -> np.ndarray:
         out = np.empty(self.n, np.int64)
         if self.lib.dcfref_parent(out.ctypes.data) != 0:

@@ -166,6 +166,11 @@ def reference_case(ref: oracle.Reference, img: np.ndarray, conn: int, tree: str)
     out["filter_ncomp_r1"] = ref.filter(17, 0.3, 1)
     out["filter_ncomp_r2"] = ref.filter(17, 0.3, 2)
     out["pattern2d_elong_area"] = ref.pattern2d(14, [1.2, 2, 4], 0, lv)
+    # CSL segmentation (perform_csl): on elongation (inertia group is current) and,
+    # after re-flooding group 0, on area
+    out["csl_elong"] = np.stack(ref.csl(14, [1.2, 2, 4]))
+    ref.check(0)
+    out["csl_area"] = np.stack(ref.csl(0, lv))
     return out
 
 
@@ -193,6 +198,15 @@ def main(refdir: str = "/root/reference") -> None:
             idx.append(int(c[0]))
             par.append(int(c[5]))
             area.append(int(c[7]))
+    with open(os.path.join(refdir, "tests", "lvec.txt")) as f:
+        next(f)
+        lvec_txt = [float(v) for v in f.read().split()]
+    oracle.build(ref=True)
+    lref = oracle.Reference()
+    lref.load(lena.astype(np.float32), 4, "max")
+    lref.check(0)
+    csl_lena = lref.csl(0, lvec_txt)
+    del lref
     np.savez_compressed(
         os.path.join(HERE, "lena_fixtures.npz"),
         lena=lena, gt_area_200=gt_area, gt_ncomp_0_2=gt_ncomp,
@@ -203,7 +217,11 @@ def main(refdir: str = "/root/reference") -> None:
         # SHA-256, length and a few lines (header, first rows, last rows)
         tree_txt_sha256=np.frombuffer(hashlib.sha256(tree_bytes).digest(), np.uint8),
         tree_txt_bytes=np.int64(len(tree_bytes)),
-        tree_txt_sample=np.array([l.decode() for l in tree_lines[:4] + tree_lines[-3:-1]]))
+        tree_txt_sample=np.array([l.decode() for l in tree_lines[:4] + tree_lines[-3:-1]]),
+        # CSL segmentation of the fixture image, area attribute, lambdas of the
+        # reference's tests/lvec.txt, 4-connectivity max-tree
+        csl_lvec=np.array(lvec_txt, np.float64),
+        csl_area_c4=np.stack(csl_lena))
 
     oracle.build(ref=True)
     ref = oracle.Reference()

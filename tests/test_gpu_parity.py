@@ -68,6 +68,13 @@ def test_tree_export_matches_reference_tree_file(ctx, lena, tmp_path):
     assert hashlib.sha256(data).digest() == bytes(lena["tree_txt_sha256"])
 
 
+def test_lena_csl_matches_reference(ctx, lena):
+    t = gpu_tree(ctx, lena["lena"], 4)
+    got = t.csl(0, dcf.lvec_from_values(lena["csl_lvec"]))
+    for i, name in enumerate(("contrast", "scale", "luminance")):
+        assert np.array_equal(got[i], lena["csl_area_c4"][i].reshape(got[i].shape)), name
+
+
 def test_lena_tree_matches_reference_tree_file(ctx, lena):
     t = gpu_tree(ctx, lena["lena"], 4)
     par = t.parent()
@@ -90,6 +97,11 @@ def test_synthetic_reference_outputs(ctx, synthetic, name):
     for rule in range(4):
         assert np.array_equal(t.filter(0, 12.0, rule), c[f"filter_area_r{rule}"]), rule
     assert np.array_equal(t.filter(0, 12.0, 0, extract=True), c["extract_area"])
+    # CSL segmentation, bit-exact (float dh sums in the reference's top-down order)
+    got = np.stack([x.reshape(-1) for x in t.csl(0, dcf.lvec_from_values([2, 5, 10, 50, 200]))])
+    assert np.array_equal(got, c["csl_area"].reshape(3, -1)), "csl area"
+    got = np.stack([x.reshape(-1) for x in t.csl(14, dcf.lvec_from_values([1.2, 2, 4]))])
+    assert np.array_equal(got, c["csl_elong"].reshape(3, -1)), "csl elongation"
     lv = dcf.lvec_from_values([2, 5, 10, 50, 200])
     assert np.array_equal(t.pattern_spectrum(0, lv), c["pattern_area"])
     exact = img.dtype != np.float32
