@@ -387,6 +387,7 @@ static void attr_carve(AttrBufs &a, int group, bool exact_g, bool has_z, size_t 
     a.group = group;
     a.exact_g = exact_g;
     a.has_z = has_z;
+    a.grey = group == 3;  // the inertia group adds them only on request (compute_attributes)
     auto take64 = [&]() { void *p = m; m += 8 * N; return p; };
     if (group == 2) for (int d = 0; d < 3; d++) a.s1[d] = (unsigned long long *)take64();
     if (group == 4) {
@@ -415,10 +416,12 @@ static cudaError_t attr_zero(const AttrBufs &a, size_t N, void *mem, int sm, cud
 }
 
 // allocate and accumulate the records of attr_idx's group
-static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
+// need_grey: the inertia group must also accumulate the grey-weighted sums (the
+// tree file's weighted centroids); its attributes 13-17 do not read them
+static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx, bool need_grey = false)
 {
     const int group = ATTR_GROUP[attr_idx];
-    if (t->attr_mem && t->attr.group == group) {
+    if (t->attr_mem && t->attr.group == group && (!need_grey || t->attr.grey)) {
         t->attr_idx = attr_idx;
         return DCF_OK;
     }
@@ -427,6 +430,7 @@ static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx)
     CU(cudaMallocAsync(&t->attr_mem, attr_bytes(group, N), ctx->stream));
     AttrBufs &a = t->attr;
     attr_carve(a, group, t->dtype == U8 || t->dtype == U16, t->g.D > 1, N, t->attr_mem);
+    if (need_grey) a.grey = true;
     CU(attr_zero(a, N, t->attr_mem, ctx->sm_count, ctx->stream));
     unsigned *count = ctx->d_err + 2;
     launch_attributes(view_of(t), a, count, ctx->up_steps, ctx->d_err, ctx->sm_count, ctx->stream);
@@ -755,10 +759,11 @@ dcf_status dcf_tree_export(dcf_ctx *ctx, dcf_tree *t, int attr_idx, const char *
         return set_err(ctx, DCF_ERR_STATE, "attribute %d is not in the tree's group (use dcf_tree_set_attribute)",
                        attr_idx);
     const int group = ATTR_GROUP[attr_idx];
+    dcf_status st;
+    if (group == 4 && (st = compute_attributes(ctx, t, attr_idx, true)) != DCF_OK) return st;
     const size_t N = (size_t)t->g.N;
     std::vector<int64_t> par(N);
     std::vector<float> gv(N);
-    dcf_status st;
     if ((st = dcf_tree_parent(ctx, t, par.data(), 0)) != DCF_OK) return st;
     if ((st = dcf_tree_gval(ctx, t, gv.data(), 0)) != DCF_OK) return st;
     std::vector<double> area;

@@ -60,32 +60,32 @@ __global__ void k_attr_pixels(const float *__restrict__ gval, Geom g, const int 
         if (G == 2 || G == 4) {
             atomicAdd(a.s1[0] + node, (unsigned long long)x);
             atomicAdd(a.s1[1] + node, (unsigned long long)y);
-            atomicAdd(a.s1[2] + node, (unsigned long long)z);
+            if (a.has_z) atomicAdd(a.s1[2] + node, (unsigned long long)z);
         }
         if (G == 4) {
             atomicAdd(a.s2[0] + node, (unsigned long long)x * x);
             atomicAdd(a.s2[1] + node, (unsigned long long)y * y);
-            atomicAdd(a.s2[2] + node, (unsigned long long)z * z);
             atomicAdd(a.s2[3] + node, (unsigned long long)x * y);
-            atomicAdd(a.s2[4] + node, (unsigned long long)y * z);
-            atomicAdd(a.s2[5] + node, (unsigned long long)x * z);
+            if (a.has_z) {
+                atomicAdd(a.s2[2] + node, (unsigned long long)z * z);
+                atomicAdd(a.s2[4] + node, (unsigned long long)y * z);
+                atomicAdd(a.s2[5] + node, (unsigned long long)x * z);
+            }
         }
-        if (G == 3 || G == 4) {
+        if (G == 3 || (G == 4 && a.grey)) {
             const float gv = gval[p];
             if (EXACT) {
                 long long gi = (long long)gv;
                 atomicAdd((unsigned long long *)a.gw[0] + node, (unsigned long long)gi);
-                if (G == 4) atomicAdd((unsigned long long *)a.gw[1] + node, (unsigned long long)(gi * gi));
                 atomicAdd((unsigned long long *)a.gw[2] + node, (unsigned long long)(gi * (long long)x));
                 atomicAdd((unsigned long long *)a.gw[3] + node, (unsigned long long)(gi * (long long)y));
-                atomicAdd((unsigned long long *)a.gw[4] + node, (unsigned long long)(gi * (long long)z));
+                if (a.has_z) atomicAdd((unsigned long long *)a.gw[4] + node, (unsigned long long)(gi * (long long)z));
             } else {
                 const double gd = (double)gv;
                 atomicAdd((double *)a.gw[0] + node, gd);
-                if (G == 4) atomicAdd((double *)a.gw[1] + node, gd * gd);
                 atomicAdd((double *)a.gw[2] + node, gd * (double)x);
                 atomicAdd((double *)a.gw[3] + node, gd * (double)y);
-                atomicAdd((double *)a.gw[4] + node, gd * (double)z);
+                if (a.has_z) atomicAdd((double *)a.gw[4] + node, gd * (double)z);
             }
         }
     }
@@ -121,12 +121,14 @@ __device__ __forceinline__ void fold_into(const AttrBufs &a, int u, int q)
         }
     }
     if (G == 2 || G == 4)
-        for (int d = 0; d < 3; d++) atomicAdd(a.s1[d] + q, __ldcg(a.s1[d] + u));
+        for (int d = 0; d < 3; d++)
+            if (s1_used(a, d)) atomicAdd(a.s1[d] + q, __ldcg(a.s1[d] + u));
     if (G == 4)
-        for (int d = 0; d < 6; d++) atomicAdd(a.s2[d] + q, __ldcg(a.s2[d] + u));
+        for (int d = 0; d < 6; d++)
+            if (s2_used(a, d)) atomicAdd(a.s2[d] + q, __ldcg(a.s2[d] + u));
     if (G == 3 || G == 4) {
         for (int d = 0; d < 5; d++) {
-            if (G == 3 && d == 1) continue;
+            if (!gw_used(a, d)) continue;
             if (EXACT)
                 atomicAdd((unsigned long long *)a.gw[d] + q, __ldcg((unsigned long long *)a.gw[d] + u));
             else
@@ -204,17 +206,21 @@ __device__ __forceinline__ void rest_copy(const RestRecs &dst, int i, const Attr
     if (to_rest) {
         dst.area[i] = src.area[u];
         if (G == 1) for (int d = 0; d < 3; d++) { dst.bmin[d][i] = src.bmin[d][u]; dst.bmax[d][i] = src.bmax[d][u]; }
-        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) dst.s1[d][i] = src.s1[d][u];
-        if (G == 4) for (int d = 0; d < 6; d++) dst.s2[d][i] = src.s2[d][u];
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) if (s1_used(src, d)) dst.s1[d][i] = src.s1[d][u];
+        if (G == 4) for (int d = 0; d < 6; d++) if (s2_used(src, d)) dst.s2[d][i] = src.s2[d][u];
         if (G == 3 || G == 4)
-            for (int d = 0; d < 5; d++) ((unsigned long long *)dst.gw[d])[i] = ((const unsigned long long *)src.gw[d])[u];
+            for (int d = 0; d < 5; d++)
+                if (gw_used(src, d))
+                    ((unsigned long long *)dst.gw[d])[i] = ((const unsigned long long *)src.gw[d])[u];
     } else {
         src.area[u] = dst.area[i];
         if (G == 1) for (int d = 0; d < 3; d++) { src.bmin[d][u] = dst.bmin[d][i]; src.bmax[d][u] = dst.bmax[d][i]; }
-        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) src.s1[d][u] = dst.s1[d][i];
-        if (G == 4) for (int d = 0; d < 6; d++) src.s2[d][u] = dst.s2[d][i];
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) if (s1_used(src, d)) src.s1[d][u] = dst.s1[d][i];
+        if (G == 4) for (int d = 0; d < 6; d++) if (s2_used(src, d)) src.s2[d][u] = dst.s2[d][i];
         if (G == 3 || G == 4)
-            for (int d = 0; d < 5; d++) ((unsigned long long *)src.gw[d])[u] = ((const unsigned long long *)dst.gw[d])[i];
+            for (int d = 0; d < 5; d++)
+                if (gw_used(src, d))
+                    ((unsigned long long *)src.gw[d])[u] = ((const unsigned long long *)dst.gw[d])[i];
     }
 }
 
@@ -252,8 +258,9 @@ __global__ void k_rest_links(const int *__restrict__ list, const unsigned *count
 // Reads the `in` buffers, writes `out` (initialised as a copy of `in`).
 template <int G, bool EXACT>
 __global__ void k_jump_fold(const unsigned *count, unsigned cap, const int *__restrict__ jin, int *jout, RestRecs in,
-                            RestRecs out, bool has_z)
+                            RestRecs out, AttrBufs a)
 {
+    const bool has_z = a.has_z;
     const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
         int j = jin[i];
@@ -268,11 +275,11 @@ __global__ void k_jump_fold(const unsigned *count, unsigned cap, const int *__re
                 atomicMin(out.bmin[d] + j, in.bmin[d][i]);
                 atomicMax(out.bmax[d] + j, in.bmax[d][i]);
             }
-        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) atomicAdd(out.s1[d] + j, in.s1[d][i]);
-        if (G == 4) for (int d = 0; d < 6; d++) atomicAdd(out.s2[d] + j, in.s2[d][i]);
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) if (s1_used(a, d)) atomicAdd(out.s1[d] + j, in.s1[d][i]);
+        if (G == 4) for (int d = 0; d < 6; d++) if (s2_used(a, d)) atomicAdd(out.s2[d] + j, in.s2[d][i]);
         if (G == 3 || G == 4)
             for (int d = 0; d < 5; d++) {
-                if (G == 3 && d == 1) continue;
+                if (!gw_used(a, d)) continue;
                 if (EXACT) atomicAdd((unsigned long long *)out.gw[d] + j, ((const unsigned long long *)in.gw[d])[i]);
                 else atomicAdd((double *)out.gw[d] + j, ((const double *)in.gw[d])[i]);
             }
@@ -290,16 +297,17 @@ __global__ void k_rest_scatter(const int *__restrict__ list, const unsigned *cou
 
 // out = in over the first min(count, cap) records (device-side length)
 template <int G>
-__global__ void k_copy_recs(const unsigned *count, unsigned cap, RestRecs in, RestRecs out)
+__global__ void k_copy_recs(const unsigned *count, unsigned cap, RestRecs in, RestRecs out, AttrBufs a)
 {
     const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
         out.area[i] = in.area[i];
         if (G == 1) for (int d = 0; d < 3; d++) { out.bmin[d][i] = in.bmin[d][i]; out.bmax[d][i] = in.bmax[d][i]; }
-        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) out.s1[d][i] = in.s1[d][i];
-        if (G == 4) for (int d = 0; d < 6; d++) out.s2[d][i] = in.s2[d][i];
+        if (G == 2 || G == 4) for (int d = 0; d < 3; d++) if (s1_used(a, d)) out.s1[d][i] = in.s1[d][i];
+        if (G == 4) for (int d = 0; d < 6; d++) if (s2_used(a, d)) out.s2[d][i] = in.s2[d][i];
         if (G == 3 || G == 4)
-            for (int d = 0; d < 5; d++) ((unsigned long long *)out.gw[d])[i] = ((const unsigned long long *)in.gw[d])[i];
+            for (int d = 0; d < 5; d++)
+                if (gw_used(a, d)) ((unsigned long long *)out.gw[d])[i] = ((const unsigned long long *)in.gw[d])[i];
     }
 }
 
@@ -331,18 +339,18 @@ static RestRecs carve(char *&m, int group, size_t R)
     return r;
 }
 
-static void copy_recs(const RestRecs &dst, const RestRecs &src, int group, size_t R, cudaStream_t s)
+static void copy_recs(const RestRecs &dst, const RestRecs &src, const AttrBufs &a, size_t R, cudaStream_t s)
 {
     cudaMemcpyAsync(dst.area, src.area, 4 * R, cudaMemcpyDeviceToDevice, s);
     for (int d = 0; d < 3; d++) {
         if (dst.bmin[d]) cudaMemcpyAsync(dst.bmin[d], src.bmin[d], 4 * R, cudaMemcpyDeviceToDevice, s);
         if (dst.bmax[d]) cudaMemcpyAsync(dst.bmax[d], src.bmax[d], 4 * R, cudaMemcpyDeviceToDevice, s);
-        if (dst.s1[d]) cudaMemcpyAsync(dst.s1[d], src.s1[d], 8 * R, cudaMemcpyDeviceToDevice, s);
+        if (dst.s1[d] && s1_used(a, d)) cudaMemcpyAsync(dst.s1[d], src.s1[d], 8 * R, cudaMemcpyDeviceToDevice, s);
     }
     for (int d = 0; d < 6; d++)
-        if (dst.s2[d]) cudaMemcpyAsync(dst.s2[d], src.s2[d], 8 * R, cudaMemcpyDeviceToDevice, s);
+        if (dst.s2[d] && s2_used(a, d)) cudaMemcpyAsync(dst.s2[d], src.s2[d], 8 * R, cudaMemcpyDeviceToDevice, s);
     for (int d = 0; d < 5; d++)
-        if (dst.gw[d]) cudaMemcpyAsync(dst.gw[d], src.gw[d], 8 * R, cudaMemcpyDeviceToDevice, s);
+        if (dst.gw[d] && gw_used(a, d)) cudaMemcpyAsync(dst.gw[d], src.gw[d], 8 * R, cudaMemcpyDeviceToDevice, s);
 }
 
 #define DCF_GROUP_SWITCH(M)                                  \
@@ -410,12 +418,12 @@ static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool exact,
     RestRecs *ri = &r0, *ro = &r1;
     int *ji = j0, *jo = j1;
     for (int k = 0; k < rounds; k++) {
-        if (exact) copy_recs(*ro, *ri, G, cap, s);
+        if (exact) copy_recs(*ro, *ri, a, cap, s);
         else {
-            k_copy_recs<G><<<rb, 256, 0, s>>>(count, cap, *ri, *ro);
+            k_copy_recs<G><<<rb, 256, 0, s>>>(count, cap, *ri, *ro, a);
             note_launch();
         }
-        k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, cap, ji, jo, *ri, *ro, a.has_z); note_launch();
+        k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, cap, ji, jo, *ri, *ro, a); note_launch();
         RestRecs *tr = ri; ri = ro; ro = tr;
         int *tj = ji; ji = jo; jo = tj;
     }

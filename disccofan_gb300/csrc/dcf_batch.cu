@@ -190,18 +190,16 @@ __global__ void k_batch_attr_pixels(const float *__restrict__ gval, Geom bg, con
             atomicAdd(a.s2[1] + node, (unsigned long long)y * y);
             atomicAdd(a.s2[3] + node, (unsigned long long)x * y);
         }
-        if (G == 3 || G == 4) {
+        if (G == 3 || (G == 4 && a.grey)) {
             const float gv = gval[p];
             if (EXACT) {
                 const long long gi = (long long)gv;
                 atomicAdd((unsigned long long *)a.gw[0] + node, (unsigned long long)gi);
-                if (G == 4) atomicAdd((unsigned long long *)a.gw[1] + node, (unsigned long long)(gi * gi));
                 atomicAdd((unsigned long long *)a.gw[2] + node, (unsigned long long)(gi * (long long)x));
                 atomicAdd((unsigned long long *)a.gw[3] + node, (unsigned long long)(gi * (long long)y));
             } else {
                 const double gd = (double)gv;
                 atomicAdd((double *)a.gw[0] + node, gd);
-                if (G == 4) atomicAdd((double *)a.gw[1] + node, gd * gd);
                 atomicAdd((double *)a.gw[2] + node, gd * (double)x);
                 atomicAdd((double *)a.gw[3] + node, gd * (double)y);
             }

@@ -122,7 +122,19 @@ struct AttrBufs {
     unsigned long long *s2[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // x2 y2 z2 xy yz xz
     void *gw[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // sum g, g^2, g*x, g*y, g*z (i64 or f64)
     int *pending = nullptr;          // children not yet folded in (bottom-up pass)
+    bool grey = true;                // inertia group: accumulate the grey-weighted sums too
 };
+
+// Fields a pass must move: z moments only in 3-D; grey-weighted sums for the wmean
+// group, and for the inertia group only when asked (its attributes 13-17 use the
+// geometric moments alone; the sums feed the tree file's weighted centroids); the
+// sum of squared grey levels is read by no attribute.
+__host__ __device__ inline bool s1_used(const AttrBufs &a, int d) { return d < 2 || a.has_z; }
+__host__ __device__ inline bool s2_used(const AttrBufs &a, int d) { return d == 0 || d == 1 || d == 3 || a.has_z; }
+__host__ __device__ inline bool gw_used(const AttrBufs &a, int d)
+{
+    return (a.group == 3 || (a.group == 4 && a.grey)) && d != 1 && (d != 4 || a.has_z);
+}
 
 struct TreeView {
     Geom g;
