@@ -377,7 +377,7 @@ static size_t attr_bytes(int group, size_t N)
 {
     const size_t n32 = 1 + 1 + (group == 1 ? 6 : 0);                                  // area, pending, bbox
     const size_t n64 = (group == 2 ? 3 : 0) + (group == 3 ? 5 : 0) + (group == 4 ? 14 : 0);
-    return (n32 * 4 + n64 * 8) * N + 256;
+    return (n32 * 4 + n64 * 8 + 1) * N + 256;  // + one `single` byte per pixel
 }
 
 static void attr_carve(AttrBufs &a, int group, bool exact_g, bool has_z, size_t N, void *mem)
@@ -402,6 +402,7 @@ static void attr_carve(AttrBufs &a, int group, bool exact_g, bool has_z, size_t 
         for (int d = 0; d < 3; d++) a.bmin[d] = (uint32_t *)take32();
         for (int d = 0; d < 3; d++) a.bmax[d] = (uint32_t *)take32();
     }
+    a.single = (unsigned char *)m;
 }
 
 // zero every record, bounding-box minima to all-ones, 2-D z extent to [0, 1)

@@ -6,7 +6,8 @@
 //                  coordinate and grey-weighted moments) to its node's record;
 //                  area updates are warp-aggregated (lanes of one flat zone add once).
 //                  Level roots count their children in `pending`.
-//   k_mark_leaves  nodes without children are tagged (pending = -1).
+//   k_mark_leaves  nodes without children are tagged (pending = -1), nodes with
+//                  one child flagged (`single`).
 //   k_attr_up      bottom-up fold: a thread starts at every leaf, adds its record
 //                  into the parent, and only the thread that brings a parent's
 //                  pending count to zero continues upward with the completed record.
@@ -103,46 +104,115 @@ void launch_fill_u32(long long n, uint32_t *dst, uint32_t v, int sm, cudaStream_
     k_fill_u32<<<grid_for(n, 256, sm), 256, 0, s>>>(n, dst, v); note_launch();
 }
 
-__global__ void k_mark_leaves(long long n, const unsigned char *__restrict__ isroot, int *pending)
+// leaves get pending = -1; nodes with exactly one child are flagged in `single`
+__global__ void k_mark_leaves(long long n, const unsigned char *__restrict__ isroot, int *pending,
+                              unsigned char *single)
 {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-         p += (long long)gridDim.x * blockDim.x)
-        if (isroot[p] && pending[p] == 0) pending[p] = -1;
+         p += (long long)gridDim.x * blockDim.x) {
+        if (!isroot[p]) continue;
+        const int c = pending[p];
+        if (c == 0) pending[p] = -1;
+        single[p] = c == 1;
+    }
 }
 
+// One node's record in registers (the fields the group uses).
 template <int G, bool EXACT>
-__device__ __forceinline__ void fold_into(const AttrBufs &a, int u, int q)
+struct Rec {
+    uint32_t area;
+    uint32_t bmin[3], bmax[3];
+    unsigned long long s1[3], s2[6], gw[5];  // gw: integer sums, or the bits of doubles
+};
+
+template <int G, bool EXACT>
+__device__ __forceinline__ void rec_load(const AttrBufs &a, int u, Rec<G, EXACT> &r)
 {
-    atomicAdd(a.area + q, __ldcg(a.area + u));
-    if (G == 1) {
-        for (int d = 0; d < (a.has_z ? 3 : 2); d++) {
-            atomicMin(a.bmin[d] + q, __ldcg(a.bmin[d] + u));
-            atomicMax(a.bmax[d] + q, __ldcg(a.bmax[d] + u));
+    r.area = __ldcg(a.area + u);
+    if (G == 1)
+        for (int d = 0; d < 3; d++) {
+            r.bmin[d] = __ldcg(a.bmin[d] + u);
+            r.bmax[d] = __ldcg(a.bmax[d] + u);
         }
-    }
+    if (G == 2 || G == 4)
+        for (int d = 0; d < 3; d++) r.s1[d] = s1_used(a, d) ? __ldcg(a.s1[d] + u) : 0ull;
+    if (G == 4)
+        for (int d = 0; d < 6; d++) r.s2[d] = s2_used(a, d) ? __ldcg(a.s2[d] + u) : 0ull;
+    if (G == 3 || G == 4)
+        for (int d = 0; d < 5; d++) r.gw[d] = gw_used(a, d) ? __ldcg((unsigned long long *)a.gw[d] + u) : 0ull;
+}
+
+// q's own contributions plus the carried record of its only child, stored as q's
+// complete record (nobody else writes q: its one child is this walker)
+template <int G, bool EXACT>
+__device__ __forceinline__ void rec_absorb_store(const AttrBufs &a, int q, Rec<G, EXACT> &r)
+{
+    r.area += __ldcg(a.area + q);
+    __stcg(a.area + q, r.area);
+    if (G == 1)
+        for (int d = 0; d < (a.has_z ? 3 : 2); d++) {
+            r.bmin[d] = min(r.bmin[d], __ldcg(a.bmin[d] + q));
+            r.bmax[d] = max(r.bmax[d], __ldcg(a.bmax[d] + q));
+            __stcg(a.bmin[d] + q, r.bmin[d]);
+            __stcg(a.bmax[d] + q, r.bmax[d]);
+        }
     if (G == 2 || G == 4)
         for (int d = 0; d < 3; d++)
-            if (s1_used(a, d)) atomicAdd(a.s1[d] + q, __ldcg(a.s1[d] + u));
+            if (s1_used(a, d)) {
+                r.s1[d] += __ldcg(a.s1[d] + q);
+                __stcg(a.s1[d] + q, r.s1[d]);
+            }
     if (G == 4)
         for (int d = 0; d < 6; d++)
-            if (s2_used(a, d)) atomicAdd(a.s2[d] + q, __ldcg(a.s2[d] + u));
-    if (G == 3 || G == 4) {
+            if (s2_used(a, d)) {
+                r.s2[d] += __ldcg(a.s2[d] + q);
+                __stcg(a.s2[d] + q, r.s2[d]);
+            }
+    if (G == 3 || G == 4)
         for (int d = 0; d < 5; d++) {
             if (!gw_used(a, d)) continue;
-            if (EXACT)
-                atomicAdd((unsigned long long *)a.gw[d] + q, __ldcg((unsigned long long *)a.gw[d] + u));
-            else
-                atomicAdd((double *)a.gw[d] + q, __ldcg((double *)a.gw[d] + u));
+            unsigned long long *f = (unsigned long long *)a.gw[d] + q;
+            if (EXACT) r.gw[d] += __ldcg(f);
+            else r.gw[d] = __double_as_longlong(__longlong_as_double(r.gw[d]) + __longlong_as_double(__ldcg(f)));
+            __stcg(f, r.gw[d]);
         }
-    }
+}
+
+// the carried record added into q with atomics (q has other children)
+template <int G, bool EXACT>
+__device__ __forceinline__ void rec_fold(const AttrBufs &a, int q, const Rec<G, EXACT> &r)
+{
+    atomicAdd(a.area + q, r.area);
+    if (G == 1)
+        for (int d = 0; d < (a.has_z ? 3 : 2); d++) {
+            atomicMin(a.bmin[d] + q, r.bmin[d]);
+            atomicMax(a.bmax[d] + q, r.bmax[d]);
+        }
+    if (G == 2 || G == 4)
+        for (int d = 0; d < 3; d++)
+            if (s1_used(a, d)) atomicAdd(a.s1[d] + q, r.s1[d]);
+    if (G == 4)
+        for (int d = 0; d < 6; d++)
+            if (s2_used(a, d)) atomicAdd(a.s2[d] + q, r.s2[d]);
+    if (G == 3 || G == 4)
+        for (int d = 0; d < 5; d++) {
+            if (!gw_used(a, d)) continue;
+            if (EXACT) atomicAdd((unsigned long long *)a.gw[d] + q, r.gw[d]);
+            else atomicAdd((double *)a.gw[d] + q, __longlong_as_double(r.gw[d]));
+        }
 }
 
 constexpr int STALLED = -3;         // pending value of a complete node not folded upward
 
-// Bottom-up fold limited to up_steps nodes per walker: a walker stopping at a
-// complete node marks it STALLED instead of folding it into its parent.  What is
-// left (STALLED nodes and nodes still waiting for children) lies near the root and
-// is finished by pointer jumping (k_jump_fold).
+// Bottom-up fold limited to up_steps nodes per walker, starting at the leaves and
+// carrying the current node's complete record in registers.  Into a parent with one
+// child the walker adds its record and stores the parent's total directly (no
+// atomics, no fences, the parent's count cleared); into a parent with several
+// children it folds with atomics, and the last child to arrive (pending count)
+// continues with the parent's record.  A walker stopping at a complete node marks
+// it STALLED instead of folding it into its parent.  What is left (STALLED nodes and
+// nodes still waiting for children) lies near the root and is finished by pointer
+// jumping (k_jump_fold).
 template <int G, bool EXACT>
 __global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs a, int up_steps, unsigned *err)
 {
@@ -150,19 +220,28 @@ __global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs 
          p += (long long)gridDim.x * blockDim.x) {
         if (__ldcg(a.pending + p) != -1) continue;
         int u = (int)p;
+        Rec<G, EXACT> r;
+        rec_load<G, EXACT>(a, u, r);
         for (int step = 0;; step++) {
-            int q = parent[u];
+            const int q = parent[u];
             if (q == NONE) break;
             if (step == up_steps) {
                 a.pending[u] = STALLED;
                 break;
             }
-            fold_into<G, EXACT>(a, u, q);
+            if (a.single[q]) {
+                rec_absorb_store<G, EXACT>(a, q, r);
+                a.pending[q] = 0;
+                u = q;
+                continue;
+            }
+            rec_fold<G, EXACT>(a, q, r);
             __threadfence();
-            int before = atomicSub(a.pending + q, 1);
+            const int before = atomicSub(a.pending + q, 1);
             if (before != 1) break;
             __threadfence();
             u = q;
+            rec_load<G, EXACT>(a, u, r);
         }
     }
 }
@@ -369,7 +448,7 @@ void launch_attributes_up(const TreeView &t, AttrBufs &a, unsigned *count, int u
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_ATTR_UP, s);
-    k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending); note_launch();
+    k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, a.single); note_launch();
 #define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, up_steps, err); note_launch()
     DCF_GROUP_SWITCH(DCF_UP)
 #undef DCF_UP

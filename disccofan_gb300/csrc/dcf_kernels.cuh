@@ -122,6 +122,7 @@ struct AttrBufs {
     unsigned long long *s2[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // x2 y2 z2 xy yz xz
     void *gw[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // sum g, g^2, g*x, g*y, g*z (i64 or f64)
     int *pending = nullptr;          // children not yet folded in (bottom-up pass)
+    unsigned char *single = nullptr; // node has exactly one child (bottom-up pass)
     bool grey = true;                // inertia group: accumulate the grey-weighted sums too
 };
 
