@@ -337,10 +337,12 @@ __global__ void k_rest_links(const int *__restrict__ list, const unsigned *count
 // Reads the `in` buffers, writes `out` (initialised as a copy of `in`).
 template <int G, bool EXACT>
 __global__ void k_jump_fold(const unsigned *count, unsigned cap, const int *__restrict__ jin, int *jout, RestRecs in,
-                            RestRecs out, AttrBufs a)
+                            RestRecs out, AttrBufs a, const unsigned *act, unsigned *act_next)
 {
+    if (*act == 0) return;  // an earlier round found no jump left
     const bool has_z = a.has_z;
     const unsigned R = rest_count(count, cap);
+    bool more = false;
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
         int j = jin[i];
         if (j == NONE) {
@@ -348,6 +350,7 @@ __global__ void k_jump_fold(const unsigned *count, unsigned cap, const int *__re
             continue;
         }
         jout[i] = jin[j];
+        more |= jin[j] != NONE;
         atomicAdd(out.area + j, in.area[i]);
         if (G == 1)
             for (int d = 0; d < (has_z ? 3 : 2); d++) {
@@ -363,12 +366,17 @@ __global__ void k_jump_fold(const unsigned *count, unsigned cap, const int *__re
                 else atomicAdd((double *)out.gw[d] + j, ((const double *)in.gw[d])[i]);
             }
     }
+    if (__any_sync(0xffffffffu, more) && (threadIdx.x & 31) == 0) *act_next = 1u;
 }
 
+// active rounds form a prefix; after an odd number of them the records are in r1
 template <int G>
 __global__ void k_rest_scatter(const int *__restrict__ list, const unsigned *count, unsigned cap, AttrBufs a,
-                               RestRecs r)
+                               RestRecs r0, RestRecs r1, const unsigned *act, int rounds)
 {
+    int done = 0;
+    while (done < rounds && act[done]) done++;
+    const RestRecs &r = (done & 1) ? r1 : r0;
     const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x)
         rest_copy<G>(r, (int)i, a, list[i], false);
@@ -376,8 +384,10 @@ __global__ void k_rest_scatter(const int *__restrict__ list, const unsigned *cou
 
 // out = in over the first min(count, cap) records (device-side length)
 template <int G>
-__global__ void k_copy_recs(const unsigned *count, unsigned cap, RestRecs in, RestRecs out, AttrBufs a)
+__global__ void k_copy_recs(const unsigned *count, unsigned cap, RestRecs in, RestRecs out, AttrBufs a,
+                            const unsigned *act)
 {
+    if (*act == 0) return;
     const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
         out.area[i] = in.area[i];
@@ -403,7 +413,8 @@ static size_t rest_record_bytes(int group)
 size_t attr_rest_bytes(int group, size_t R)
 {
     // list + 2 jump arrays + 2 compact record buffers (each array 256-byte aligned)
-    return 3 * ((4 * R + 255) / 256 * 256) + 2 * (rest_record_bytes(group) * R + 16 * 256) + 256;
+    // + the rounds' activity flags
+    return 3 * ((4 * R + 255) / 256 * 256) + 2 * (rest_record_bytes(group) * R + 16 * 256) + 2 * 256;
 }
 
 static RestRecs carve(char *&m, int group, size_t R)
@@ -416,20 +427,6 @@ static RestRecs carve(char *&m, int group, size_t R)
     if (group == 4) for (int d = 0; d < 6; d++) r.s2[d] = (unsigned long long *)take(8);
     if (group == 3 || group == 4) for (int d = 0; d < 5; d++) r.gw[d] = take(8);
     return r;
-}
-
-static void copy_recs(const RestRecs &dst, const RestRecs &src, const AttrBufs &a, size_t R, cudaStream_t s)
-{
-    cudaMemcpyAsync(dst.area, src.area, 4 * R, cudaMemcpyDeviceToDevice, s);
-    for (int d = 0; d < 3; d++) {
-        if (dst.bmin[d]) cudaMemcpyAsync(dst.bmin[d], src.bmin[d], 4 * R, cudaMemcpyDeviceToDevice, s);
-        if (dst.bmax[d]) cudaMemcpyAsync(dst.bmax[d], src.bmax[d], 4 * R, cudaMemcpyDeviceToDevice, s);
-        if (dst.s1[d] && s1_used(a, d)) cudaMemcpyAsync(dst.s1[d], src.s1[d], 8 * R, cudaMemcpyDeviceToDevice, s);
-    }
-    for (int d = 0; d < 6; d++)
-        if (dst.s2[d] && s2_used(a, d)) cudaMemcpyAsync(dst.s2[d], src.s2[d], 8 * R, cudaMemcpyDeviceToDevice, s);
-    for (int d = 0; d < 5; d++)
-        if (dst.gw[d] && gw_used(a, d)) cudaMemcpyAsync(dst.gw[d], src.gw[d], 8 * R, cudaMemcpyDeviceToDevice, s);
 }
 
 #define DCF_GROUP_SWITCH(M)                                  \
@@ -469,12 +466,13 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_s
     launch_attributes_up(t, a, count, up_steps, err, sm, s);
 }
 
-// Pointer-jumping phase over the nodes the walkers left.  `cap` sizes the scratch;
-// exact == true: cap is the count the caller read back (round count from it, copies
-// by cudaMemcpyAsync of that length); exact == false: the count stays on the device,
-// rounds cover any forest of up to cap nodes and copies are kernels.
+// Pointer-jumping phase over the nodes the walkers left.  `cap` sizes the scratch
+// (exact == true: the count the caller read back; false: a capacity, the count
+// staying on the device).  Enough rounds are launched for a chain of cap nodes, but
+// each round flags whether any jump is left: once none is, the remaining rounds
+// return at once (the forest is usually far shallower than its node count).
 template <int G, bool E>
-static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool exact, unsigned *count, void *scratch,
+static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool, unsigned *count, void *scratch,
                        unsigned *err, int sm, cudaStream_t s)
 {
     const int nb = grid_for(t.g.N, 256, sm);
@@ -486,6 +484,9 @@ static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool exact,
     int *j1 = (int *)m;
     m += (4 * (size_t)cap + 255) / 256 * 256;
     RestRecs r0 = carve(m, a.group, cap), r1 = carve(m, a.group, cap);
+    unsigned *act = (unsigned *)m;  // act[k] != 0: round k has work (at most 32 rounds)
+    cudaMemsetAsync(act, 0, 33 * sizeof(unsigned), s);
+    cudaMemsetAsync(act, 1, 1, s);
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
     k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, list, count, cap, err); note_launch();
     if (cap == 0) return;
@@ -497,16 +498,12 @@ static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool exact,
     RestRecs *ri = &r0, *ro = &r1;
     int *ji = j0, *jo = j1;
     for (int k = 0; k < rounds; k++) {
-        if (exact) copy_recs(*ro, *ri, a, cap, s);
-        else {
-            k_copy_recs<G><<<rb, 256, 0, s>>>(count, cap, *ri, *ro, a);
-            note_launch();
-        }
-        k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, cap, ji, jo, *ri, *ro, a); note_launch();
+        k_copy_recs<G><<<rb, 256, 0, s>>>(count, cap, *ri, *ro, a, act + k); note_launch();
+        k_jump_fold<G, E><<<rb, 256, 0, s>>>(count, cap, ji, jo, *ri, *ro, a, act + k, act + k + 1); note_launch();
         RestRecs *tr = ri; ri = ro; ro = tr;
         int *tj = ji; ji = jo; jo = tj;
     }
-    k_rest_scatter<G><<<rb, 256, 0, s>>>(list, count, cap, a, *ri); note_launch();
+    k_rest_scatter<G><<<rb, 256, 0, s>>>(list, count, cap, a, r0, r1, act, rounds); note_launch();
 }
 
 // Phase 2: R = number of nodes the walkers left (read back by the caller), scratch
