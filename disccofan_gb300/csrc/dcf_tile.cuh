@@ -123,14 +123,27 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     }
     __syncthreads();
 
-    // level-root form inside the tile (read-only walks, then each pixel writes its
-    // own word): pixel -> level root, root -> parent's level root; to global indices
+    // level-root form inside the tile: pixel -> level root, root -> parent's level
+    // root; to global indices.  Level roots by pointer doubling over the equal-key
+    // links (a flat zone of F pixels can be a chain of ~F links, so walking it from
+    // every pixel would cost O(F^2)): r(i) = parent if it has i's key, else i; then
+    // r(i) = r(r(i)) until every chain (at most WORDS long) has collapsed.
     unsigned short *sroot = sstk;  // the row stacks (>= WORDS entries) are no longer needed
     for (int i = tid; i < WORDS; i += TILE_THREADS) {
         int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
-        sroot[i] = (lx < wl && ly < hl && lz < dl) ? (unsigned short)levelroot_ro(acc, i) : (unsigned short)0xFFFFu;
+        unsigned short r = (unsigned short)i;
+        if (lx < wl && ly < hl && lz < dl) {
+            const uint64_t w = snode[i];
+            const int q = wpar(w);
+            if (q != NONE && wkey(snode[q]) == wkey(w)) r = (unsigned short)q;
+        }
+        sroot[i] = r;
     }
     __syncthreads();
+    for (int span = 1; span < WORDS; span <<= 1) {
+        for (int i = tid; i < WORDS; i += TILE_THREADS) sroot[i] = sroot[sroot[i]];
+        __syncthreads();
+    }
     for (int i = tid; i < WORDS; i += TILE_THREADS) {
         int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         if (lx >= wl || ly >= hl || lz >= dl) continue;
