@@ -37,7 +37,7 @@ static __device__ __forceinline__ Geom cut_geom(const BatchImg &im, const Geom &
 // the atomic counter *next until the list is exhausted.  Every grab advances the
 // counter, so the loop ends after at most ntiles / chunk + 1 grabs per CTA.
 template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS, 5)
+__global__ void __launch_bounds__(TileCfg<T>::threads, TileCfg<T>::min_blocks)
 k_batch_tile_build(const T *__restrict__ img, Geom bg, const BatchImg *__restrict__ imgs,
                    const BatchTile *__restrict__ tiles, int ntiles, int chunk, unsigned *next,
                    float *__restrict__ gval, unsigned long long *__restrict__ gnode, unsigned *err)
@@ -274,12 +274,11 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
                         unsigned char *isroot, unsigned long long *num_nodes, unsigned *err, int ctas_per_sm,
                         SeamEdges &seam, int sm, cudaStream_t s)
 {
-    const size_t smem = tile_smem_bytes(bg.tw, bg.th, 1);
     const int grid = sm * ctas_per_sm;
     cudaMemsetAsync(next, 0, sizeof(unsigned), s);
     prof_begin(P_TILE, s);
 #define DCF_TB(T)                                                                                       \
-    k_batch_tile_build<T><<<grid, TILE_THREADS, smem, s>>>((const T *)img, bg, imgs, tiles, ntiles, chunk, \
+    k_batch_tile_build<T><<<grid, TileCfg<T>::threads, tile_smem_bytes(bg.tw, bg.th, 1, TileCfg<T>::word_bytes), s>>>((const T *)img, bg, imgs, tiles, ntiles, chunk, \
                                                           next, gval, node, err); note_launch()
     switch (dtype) {
     case U8: DCF_TB(uint8_t); break;
@@ -349,14 +348,17 @@ namespace dcf {
 // CTAs of the persistent tile kernel that fit on one SM for a tile shape
 int batch_max_ctas_per_sm(int dtype, int tw, int th)
 {
-    const size_t smem = tile_smem_bytes(tw, th, 1);
     int n = 0;
+#define DCF_OCC(T)                                                                                       \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_tile_build<T>, TileCfg<T>::threads,      \
+                                                  tile_smem_bytes(tw, th, 1, TileCfg<T>::word_bytes))
     switch (dtype) {
-    case U8: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_tile_build<uint8_t>, TILE_THREADS, smem); break;
-    case U16: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_tile_build<uint16_t>, TILE_THREADS, smem); break;
-    case U32: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_tile_build<uint32_t>, TILE_THREADS, smem); break;
-    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_tile_build<float>, TILE_THREADS, smem); break;
+    case U8: DCF_OCC(uint8_t); break;
+    case U16: DCF_OCC(uint16_t); break;
+    case U32: DCF_OCC(uint32_t); break;
+    default: DCF_OCC(float); break;
     }
+#undef DCF_OCC
     return n;
 }
 

@@ -49,7 +49,7 @@ __global__ void k_stats(const T *__restrict__ img, long long n, unsigned *kmin, 
 }
 
 template <typename T, bool MIN>
-__global__ void __launch_bounds__(TILE_THREADS, 5)
+__global__ void __launch_bounds__(TileCfg<T>::threads, TileCfg<T>::min_blocks)
 k_tile_build(const T *__restrict__ img, Geom g, const unsigned *kmax, float *__restrict__ gval,
              unsigned long long *__restrict__ gnode, unsigned *err)
 {
@@ -313,9 +313,9 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
     const T *img = (const T *)a.img;
     const int TW = a.g.tw, TH = a.g.th, TD = a.g.td;
     dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
-    const size_t smem = tile_smem_bytes(TW, TH, TD);
+    const size_t smem = tile_smem_bytes(TW, TH, TD, TileCfg<T>::word_bytes);
     prof_begin(P_TILE, s);
-    k_tile_build<T, MIN><<<grid, TILE_THREADS, smem, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err); note_launch();
+    k_tile_build<T, MIN><<<grid, TileCfg<T>::threads, smem, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err); note_launch();
     prof_end(P_TILE, s);
     prof_begin(P_SEAM, s);
     {

@@ -208,80 +208,6 @@ __device__ __forceinline__ void levelroot_next(A &acc, int &i, uint64_t &w, int 
     acc.error(DEVERR_WALK_BOUND);
 }
 
-// Level root of i (follows equal-key links, path halving); on return i is the root
-// and w its word.  Used by connect_smem, where a second load per step is cheaper
-// than the registers that carrying the parent's word costs.
-template <class A>
-__device__ __forceinline__ void levelroot(A &acc, int &i, uint64_t &w)
-{
-    w = acc.load(i);
-    const uint32_t k = wkey(w);
-    const long long bound = acc.walk_bound();
-    for (long long it = 0; it < bound; it++) {
-        const int p = wpar(w);
-        if (p == NONE) return;
-        const uint64_t wp = acc.load(p);
-        if (wkey(wp) != k) return;
-        const int pp = wpar(wp);
-        if (pp != NONE) {
-            const uint64_t wpp = acc.load(pp);
-            if (wkey(wpp) == k) {
-                acc.store(i, wmake(k, pp));
-                i = pp;
-                w = wpp;
-                continue;
-            }
-        }
-        i = p;
-        w = wp;
-        return;
-    }
-    acc.error(DEVERR_WALK_BOUND);
-}
-
-// connect() for node words in shared memory (the in-tile merge): the same splices,
-// re-reading a parent's word at every step (shared-memory latency is a few tens of
-// cycles) to keep the tile kernel's register count, and so its occupancy, down.
-template <class A>
-__device__ __forceinline__ void connect_smem(A &acc, int a, int b, long long bound)
-{
-    uint64_t wa, wb;
-    levelroot(acc, a, wa);
-    levelroot(acc, b, wb);
-    for (long long it = 0; it < bound; it++) {
-        if (a == b) return;
-        uint32_t ka = wkey(wa), kb = wkey(wb);
-        if (ka < kb || (ka == kb && a < b)) {
-            int t = a; a = b; b = t;
-            uint64_t tw = wa; wa = wb; wb = tw;
-            uint32_t tk = ka; ka = kb; kb = tk;
-        }
-        const int pa = wpar(wa);
-        int lpa = pa;
-        uint64_t wl = 0;
-        if (pa != NONE) {
-            levelroot(acc, lpa, wl);
-            if (lpa == b) return;
-            if (wkey(wl) >= kb) {
-                a = lpa;
-                wa = wl;
-                continue;
-            }
-        }
-        if (acc.cas(a, wa, wmake(ka, b))) {
-            if (pa == NONE) return;
-            a = b;
-            wa = wb;
-            b = lpa;
-            wb = wl;
-        } else {
-            levelroot(acc, a, wa);
-            levelroot(acc, b, wb);
-        }
-    }
-    acc.error(DEVERR_MERGE_BOUND);
-}
-
 // Every (x, wx) pair below is read in the order word of x, then word of its parent
 // (nx, nwx); a pair may be older than other threads' writes, like the view of a
 // delayed thread, and structure only changes through a CAS on the exact word held.

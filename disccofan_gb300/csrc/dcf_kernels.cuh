@@ -17,16 +17,27 @@ void prof_end(int id, cudaStream_t s);
 // (dcf_ctx_launch_count); every launch site calls it right after the launch
 void note_launch();
 
-constexpr int TILE_THREADS = 256;
+constexpr int TILE_THREADS = 256;        // tile build CTAs with 64-bit shared node words (u32/f32)
+constexpr int TILE_THREADS_NARROW = 128; // with 32-bit words (u8/u16): more tiles resident per SM
 constexpr int TILE_MAX_PIX = 4096;             // largest build tile (16-bit local indices)
 constexpr long long MERGE_BOUND_SMEM = 1LL << 22;
 constexpr long long MERGE_BOUND_GLOBAL = 1LL << 28;
 
-// dynamic shared memory of one tile build (padded node words + padded row stacks)
-inline size_t tile_smem_bytes(int tw, int th, int td)
+// dynamic shared memory of one tile build (padded node words + padded row stacks);
+// word_bytes 8 (u32/f32 images) or 4 (u8/u16: 16-bit level and parent)
+inline size_t tile_smem_bytes(int tw, int th, int td, int word_bytes = 8)
 {
-    return (size_t)(tw + 1) * th * td * 8 + (size_t)(tw + 2) * th * td * 2;
+    return (size_t)(tw + 1) * th * td * word_bytes + (size_t)(tw + 2) * th * td * 2;
 }
+// launch shape of the tile kernels per pixel type: u8/u16 tiles use 32-bit shared
+// words and 128-thread CTAs (25 KB for 64x64: 8 resident per SM), u32/f32 tiles
+// 64-bit words and 256 threads (50 KB: 4 per SM)
+template <typename T> struct TileCfg {
+    static constexpr bool narrow = sizeof(T) <= 2;
+    static constexpr int threads = narrow ? TILE_THREADS_NARROW : TILE_THREADS;
+    static constexpr int min_blocks = narrow ? 8 : 5;
+    static constexpr int word_bytes = narrow ? 4 : 8;
+};
 
 inline int grid_for(long long n, int block, int sm_count)
 {

@@ -9,59 +9,154 @@ namespace dcf {
 // ---------------------------------------------------------------------------
 // tile build
 // ---------------------------------------------------------------------------
+// Shared-memory node words.  Word64: order key (high 32 bits) and local parent
+// (low 32, 0xFFFFFFFF = none), for u32/f32 images.  Word32: 16-bit level and 16-bit
+// local parent (0xFFFF = none), for u8/u16 images, whose levels are integers below
+// 2^16: half the shared memory per tile, so more tiles are resident per SM.
+struct Word64 {
+    using T = unsigned long long;
+    static constexpr unsigned NO = 0xFFFFFFFFu;
+    __device__ static uint32_t key(T w) { return (uint32_t)(w >> 32); }
+    __device__ static int par(T w) { return (uint32_t)w == NO ? NONE : (int)(uint32_t)w; }
+    __device__ static T make(uint32_t k, int p) { return ((T)k << 32) | (p == NONE ? NO : (uint32_t)p); }
+};
+struct Word32 {
+    using T = unsigned int;
+    static constexpr unsigned NO = 0xFFFFu;
+    __device__ static uint32_t key(T w) { return w >> 16; }
+    __device__ static int par(T w) { return (w & NO) == NO ? NONE : (int)(w & NO); }
+    __device__ static T make(uint32_t k, int p) { return (k << 16) | (p == NONE ? NO : (unsigned)p); }
+};
+template <typename T> struct TileWord { using W = Word64; };
+template <> struct TileWord<uint8_t> { using W = Word32; };
+template <> struct TileWord<uint16_t> { using W = Word32; };
+
+template <class W>
 struct SmemAcc {
-    unsigned long long *w;
+    typename W::T *w;
     unsigned *err;
     int npix;
-    __device__ uint64_t load(int i) const { return ((volatile unsigned long long *)w)[i]; }
-    __device__ void store(int i, uint64_t v) { ((volatile unsigned long long *)w)[i] = v; }
-    __device__ bool cas(int i, uint64_t expect, uint64_t v) { return atomicCAS(w + i, expect, v) == expect; }
-    __device__ long long walk_bound() const { return npix + 1; }
+    __device__ typename W::T load(int i) const { return ((volatile typename W::T *)w)[i]; }
+    __device__ void store(int i, typename W::T v) { ((volatile typename W::T *)w)[i] = v; }
+    __device__ bool cas(int i, typename W::T expect, typename W::T v) { return atomicCAS(w + i, expect, v) == expect; }
     __device__ void error(unsigned bit) { raise_error(err, bit); }
 };
+
+// Level root of i (follows equal-key links, path halving); on return i is the root
+// and w its word.
+template <class W>
+__device__ __forceinline__ void levelroot_s(SmemAcc<W> &acc, int &i, typename W::T &w)
+{
+    w = acc.load(i);
+    const uint32_t k = W::key(w);
+    for (int it = 0; it <= acc.npix; it++) {
+        const int p = W::par(w);
+        if (p == NONE) return;
+        const typename W::T wp = acc.load(p);
+        if (W::key(wp) != k) return;
+        const int pp = W::par(wp);
+        if (pp != NONE) {
+            const typename W::T wpp = acc.load(pp);
+            if (W::key(wpp) == k) {
+                acc.store(i, W::make(k, pp));
+                i = pp;
+                w = wpp;
+                continue;
+            }
+        }
+        i = p;
+        w = wp;
+        return;
+    }
+    acc.error(DEVERR_WALK_BOUND);
+}
+
+// connect() on the tile's shared-memory words (the same splices as the HBM
+// version, re-reading a parent's word at each step: shared-memory latency is a few
+// tens of cycles, and carrying it would cost registers and so occupancy)
+template <class W>
+__device__ __forceinline__ void connect_s(SmemAcc<W> &acc, int a, int b, long long bound)
+{
+    typename W::T wa, wb;
+    levelroot_s(acc, a, wa);
+    levelroot_s(acc, b, wb);
+    for (long long it = 0; it < bound; it++) {
+        if (a == b) return;
+        uint32_t ka = W::key(wa), kb = W::key(wb);
+        if (ka < kb || (ka == kb && a < b)) {
+            int t = a; a = b; b = t;
+            typename W::T tw = wa; wa = wb; wb = tw;
+            uint32_t tk = ka; ka = kb; kb = tk;
+        }
+        const int pa = W::par(wa);
+        int lpa = pa;
+        typename W::T wl = 0;
+        if (pa != NONE) {
+            levelroot_s(acc, lpa, wl);
+            if (lpa == b) return;
+            if (W::key(wl) >= kb) {
+                a = lpa;
+                wa = wl;
+                continue;
+            }
+        }
+        if (acc.cas(a, wa, W::make(ka, b))) {
+            if (pa == NONE) return;
+            a = b;
+            wa = wb;
+            b = lpa;
+            wb = wl;
+        } else {
+            levelroot_s(acc, a, wa);
+            levelroot_s(acc, b, wb);
+        }
+    }
+    acc.error(DEVERR_MERGE_BOUND);
+}
 
 // Max-tree of one tile by the whole CTA.  The tile starts at (x0, y0, z0) of an
 // image of geometry g whose pixel (x, y, z) has global index off + z*WH + y*W + x
 // (off > 0 for one cutout of a batch).  Writes gval and the tile forest
-// (level-root form, global indices) into gnode.
+// (level-root form, global indices, 64-bit order-key words) into gnode.
 //
 // Shared-memory layout (tile_smem_bytes): node words with a padded row stride
 // RS = tw + 1 (local index of pixel (lx, ly, lz) = lx + ly*RS + lz*RS*th), then one
 // stack per row with stride tw + 2 entries.  The row pass runs one row per thread
-// in lock-step; unpadded strides of tw words would put all 32 rows of a warp in
-// the same shared-memory bank at every step.
+// in lock-step; unpadded strides would put the rows of a warp in one bank.
 template <typename T, bool MIN>
 __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long off, const Geom &g, int x0, int y0,
                                            int z0, float gmax, float *__restrict__ gval,
-                                           unsigned long long *__restrict__ gnode, unsigned *err,
-                                           unsigned long long *smem_tile)
+                                           unsigned long long *__restrict__ gnode, unsigned *err, void *smem_raw)
 {
+    using W = typename TileWord<T>::W;
+    using WT = typename W::T;
+    constexpr bool NARROW = sizeof(WT) == 4;
     // tile extents from the geometry (at most 4096 pixels: local indices < 2^16)
     const bool is3d = g.D > 1;
     const int TW = g.tw, TH = g.th, TD = g.td;
     const int RS = TW + 1, SS = TW + 2, SLICE = RS * TH, WORDS = RS * TH * TD;
-    unsigned long long *snode = smem_tile;                            // WORDS node words
-    unsigned short *sstk = (unsigned short *)(smem_tile + WORDS);     // one stack per row
+    WT *snode = (WT *)smem_raw;                                        // WORDS node words
+    unsigned short *sstk = (unsigned short *)(snode + WORDS);          // one stack per row
     const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, NT = blockDim.x;
 
-    for (int i = tid; i < WORDS; i += TILE_THREADS) {
+    for (int i = tid; i < WORDS; i += NT) {
         int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         uint32_t k = 0;
         if (lx < wl && ly < hl && lz < dl) {
             long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
             float lv = level_of<T, MIN>(img[gp], gmax);
             gval[gp] = lv;
-            k = order_key(lv);
+            k = NARROW ? (uint32_t)lv : order_key(lv);  // u8/u16 levels are integers in [0, 65535]
         }
-        snode[i] = wmake(k, NONE);
+        snode[i] = W::make(k, NONE);
     }
     __syncthreads();
 
     // 1-D max-tree of each row with a stack (pop higher keys; the popped chain
     // hangs off the next popped element, the last one off the new pixel).
     const int nrows = TH * TD;
-    for (int r = tid; r < nrows; r += TILE_THREADS) {
+    for (int r = tid; r < nrows; r += NT) {
         int ly = r % TH, lz = r / TH;
         if (ly >= hl || lz >= dl) continue;
         unsigned short *stk = sstk + r * SS;
@@ -69,21 +164,21 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
         const int base = r * RS;
         for (int lx = 0; lx < wl; lx++) {
             int i = base + lx;
-            uint32_t ki = wkey(snode[i]);
+            uint32_t ki = W::key(snode[i]);
             int last = NONE;
-            while (sp > 0 && wkey(snode[stk[sp - 1]]) > ki) {
+            while (sp > 0 && W::key(snode[stk[sp - 1]]) > ki) {
                 int t = stk[--sp];
-                if (last != NONE) snode[last] = wmake(wkey(snode[last]), t);
+                if (last != NONE) snode[last] = W::make(W::key(snode[last]), t);
                 last = t;
             }
-            if (last != NONE) snode[last] = wmake(wkey(snode[last]), i);
+            if (last != NONE) snode[last] = W::make(W::key(snode[last]), i);
             stk[sp++] = (unsigned short)i;
         }
-        for (int j = sp - 1; j >= 1; j--) snode[stk[j]] = wmake(wkey(snode[stk[j]]), stk[j - 1]);
+        for (int j = sp - 1; j >= 1; j--) snode[stk[j]] = W::make(W::key(snode[stk[j]]), stk[j - 1]);
     }
     __syncthreads();
 
-    SmemAcc acc{snode, err, WORDS};
+    SmemAcc<W> acc{snode, err, WORDS};
     const Offs offs = forward_offsets(g.conn);
     // merge row bands along y (each z slice), then slabs along z; at level k the
     // seams are the rows (slices) c with c % 2^(k+1) == 2^k
@@ -95,7 +190,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
             // all edges across the seams of this level at once; correctness does not
             // depend on the order (see connect)
             const long long work = (long long)nseams * other * TW;
-            for (long long w = tid; w < work; w += TILE_THREADS) {
+            for (long long w = tid; w < work; w += NT) {
                 int lx = (int)(w % TW);
                 long long rest = w / TW;
                 int o = (int)(rest % other);
@@ -113,7 +208,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
                     if (!crosses) continue;
                     int qx = lx - dx, qy = ly - dy, qz = lz - dz;
                     if (qx < 0 || qx >= wl || qy < 0 || qy >= hl || qz < 0 || qz >= dl) continue;
-                    connect_smem(acc, p, qx + qy * RS + qz * SLICE, MERGE_BOUND_SMEM);
+                    connect_s(acc, p, qx + qy * RS + qz * SLICE, MERGE_BOUND_SMEM);
                 }
             }
             // levels are ordered for shorter merge walks, not for correctness:
@@ -129,28 +224,28 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     // every pixel would cost O(F^2)): r(i) = parent if it has i's key, else i; then
     // r(i) = r(r(i)) until every chain (at most WORDS long) has collapsed.
     unsigned short *sroot = sstk;  // the row stacks (>= WORDS entries) are no longer needed
-    for (int i = tid; i < WORDS; i += TILE_THREADS) {
+    for (int i = tid; i < WORDS; i += NT) {
         int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         unsigned short r = (unsigned short)i;
         if (lx < wl && ly < hl && lz < dl) {
-            const uint64_t w = snode[i];
-            const int q = wpar(w);
-            if (q != NONE && wkey(snode[q]) == wkey(w)) r = (unsigned short)q;
+            const WT w = snode[i];
+            const int q = W::par(w);
+            if (q != NONE && W::key(snode[q]) == W::key(w)) r = (unsigned short)q;
         }
         sroot[i] = r;
     }
     __syncthreads();
     for (int span = 1; span < WORDS; span <<= 1) {
-        for (int i = tid; i < WORDS; i += TILE_THREADS) sroot[i] = sroot[sroot[i]];
+        for (int i = tid; i < WORDS; i += NT) sroot[i] = sroot[sroot[i]];
         __syncthreads();
     }
-    for (int i = tid; i < WORDS; i += TILE_THREADS) {
+    for (int i = tid; i < WORDS; i += NT) {
         int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         if (lx >= wl || ly >= hl || lz >= dl) continue;
-        const uint64_t w = snode[i];
+        const WT w = snode[i];
         int p = sroot[i];
         if (p == i) {  // level root: its parent node's level root
-            const int q = wpar(w);
+            const int q = W::par(w);
             p = q == NONE ? NONE : (int)sroot[q];
         }
         int out = NONE;
@@ -159,7 +254,8 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
             out = (int)(off + (long long)(z0 + pz) * g.WH + (long long)(y0 + py) * g.W + (x0 + px));
         }
         long long gp = off + (long long)(z0 + lz) * g.WH + (long long)(y0 + ly) * g.W + (x0 + lx);
-        gnode[gp] = wmake(wkey(w), out);
+        const uint32_t key = NARROW ? order_key((float)W::key(w)) : W::key(w);
+        gnode[gp] = wmake(key, out);
     }
 }
 
