@@ -63,9 +63,11 @@ k_batch_tile_build(const T *__restrict__ img, Geom bg, const BatchImg *__restric
 // the tile's +x, -x and +y faces; face f takes the offsets pointing out through
 // it.  2-D forward offsets never point to -y, so every edge between two tiles of
 // one cutout leaves its low endpoint's tile through one of these faces.  Edges
-// leaving the cutout are skipped.  One connect per edge and thread.
+// leaving the cutout are skipped, and so are diagonal edges implied by others
+// (edge_implied).  One connect per edge and thread.
 __device__ __forceinline__ bool batch_seam_item(const Geom &bg, const BatchImg *imgs, const BatchTile *tiles,
-                                                const Offs &offs, int fmax, long long w, int &p, int &q)
+                                                const Offs &offs, int fmax, long long w,
+                                                const unsigned long long *gnode, int &p, int &q)
 {
     const int e = (int)(w % offs.n);
     long long r = w / offs.n;
@@ -85,6 +87,12 @@ __device__ __forceinline__ bool batch_seam_item(const Geom &bg, const BatchImg *
     if (qx < 0 || qx >= im.W || qy >= im.H) return false;
     p = (int)(im.off + (long long)y * im.W + x);
     q = (int)(im.off + (long long)qy * im.W + qx);
+    if (offs.n > 3) {
+        const unsigned kp = wkey(gnode[p]), kq = wkey(gnode[q]);
+        const int pp = p, W = im.W;
+        auto key_at = [&](int sx, int sy, int) { return wkey(gnode[pp + (long long)sy * W + sx]); };
+        if (edge_implied(dx, dy, 0, kp < kq ? kp : kq, key_at)) return false;
+    }
     return true;
 }
 
@@ -98,7 +106,7 @@ __global__ void k_batch_seam(unsigned long long *gnode, Geom bg, const BatchImg 
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
          w += (long long)gridDim.x * blockDim.x) {
         int p, q;
-        if (batch_seam_item(bg, imgs, tiles, offs, fmax, w, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
+        if (batch_seam_item(bg, imgs, tiles, offs, fmax, w, gnode, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
     }
 }
 
@@ -112,7 +120,7 @@ __global__ void k_batch_seam_collect(const unsigned long long *gnode, Geom bg, c
     for (long long base = blockIdx.x * (long long)blockDim.x + threadIdx.x - lane; base < work;
          base += (long long)gridDim.x * blockDim.x) {
         int p = 0, q = 0;
-        const bool valid = base + lane < work && batch_seam_item(bg, imgs, tiles, offs, fmax, base + lane, p, q);
+        const bool valid = base + lane < work && batch_seam_item(bg, imgs, tiles, offs, fmax, base + lane, gnode, p, q);
         seam_append(e, gnode, valid, p, q);
     }
 }

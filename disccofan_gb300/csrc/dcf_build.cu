@@ -82,9 +82,10 @@ __host__ __device__ inline long long seam_items(const Geom &g, long long ntiles)
     return ntiles * 5 * seam_face_pixels(g) * forward_offsets(g.conn).n;
 }
 
-// decode work item w into an edge (p, q); false if the item holds none
+// decode work item w into an edge (p, q); false if the item holds none or the edge
+// is implied by others (edge_implied; keys read from the tile builds' words)
 __device__ __forceinline__ bool seam_item(const Geom &g, int ntx, int nty, const Offs &offs, int fmax, long long w,
-                                          int &p, int &q)
+                                          const unsigned long long *gnode, int &p, int &q)
 {
     const int TW = g.tw, TH = g.th, TD = g.td;
     const int e = (int)(w % offs.n);
@@ -110,6 +111,14 @@ __device__ __forceinline__ bool seam_item(const Geom &g, int ntx, int nty, const
     if (qx < 0 || qx >= g.W || qy < 0 || qy >= g.H || qz >= g.D) return false;
     p = (int)((long long)z * g.WH + (long long)y * g.W + x);
     q = (int)((long long)qz * g.WH + (long long)qy * g.W + qx);
+    if (offs.n > 3) {
+        const unsigned kp = wkey(gnode[p]), kq = wkey(gnode[q]);
+        const int pp = p;
+        auto key_at = [&](int sx, int sy, int sz) {
+            return wkey(gnode[pp + (long long)sz * g.WH + (long long)sy * g.W + sx]);
+        };
+        if (edge_implied(dx, dy, dz, kp < kq ? kp : kq, key_at)) return false;
+    }
     return true;
 }
 
@@ -123,7 +132,7 @@ __global__ void k_seam_direct(unsigned long long *gnode, Geom g, int ntx, int nt
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
          w += (long long)gridDim.x * blockDim.x) {
         int p, q;
-        if (seam_item(g, ntx, nty, offs, fmax, w, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
+        if (seam_item(g, ntx, nty, offs, fmax, w, gnode, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
     }
 }
 
@@ -137,7 +146,7 @@ __global__ void k_seam_collect(const unsigned long long *gnode, Geom g, int ntx,
     for (long long base = blockIdx.x * (long long)blockDim.x + threadIdx.x - lane; base < work;
          base += (long long)gridDim.x * blockDim.x) {
         int p = 0, q = 0;
-        const bool valid = base + lane < work && seam_item(g, ntx, nty, offs, fmax, base + lane, p, q);
+        const bool valid = base + lane < work && seam_item(g, ntx, nty, offs, fmax, base + lane, gnode, p, q);
         seam_append(e, gnode, valid, p, q);
     }
 }

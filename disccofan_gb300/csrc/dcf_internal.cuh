@@ -108,6 +108,28 @@ __host__ __device__ inline Offs forward_offsets(int conn)
     return o;
 }
 
+// Edges implied by others.  An edge from p to q = p + (ex, ey, ez) with two or three
+// non-zero components can be left out when some pixel r = p + s, s a proper part of
+// the offset (some of its non-zero components, not all), has level >= min(level p,
+// level q): the path p - r - q is made of two edges with fewer non-zero components
+// and joins p and q at every threshold at or below the edge's level, so the max-tree
+// is the same without the edge.  Straight edges are never left out, so by induction
+// over the number of non-zero components every dropped edge is implied by kept ones,
+// whichever phase (row pass, band merge, seam merge) handles those.  The 8- and
+// 26-neighbourhoods hold every part of each of their offsets.  key_at(sx, sy, sz)
+// returns the order key of pixel p + (sx, sy, sz).
+template <class KeyAt>
+__device__ __forceinline__ bool edge_implied(int ex, int ey, int ez, uint32_t kmin, KeyAt key_at)
+{
+    const int nz = (ex != 0) | ((ey != 0) << 1) | ((ez != 0) << 2);
+    if (__popc(nz) < 2) return false;
+    for (int m = 1; m < 7; m++) {
+        if ((m & ~nz) || m == nz) continue;
+        if (key_at(m & 1 ? ex : 0, m & 2 ? ey : 0, m & 4 ? ez : 0) >= kmin) return true;
+    }
+    return false;
+}
+
 // ---------------------------------------------------------------------------
 // Lock-free concurrent merge of two branches of a max-tree forest.
 //

@@ -208,7 +208,15 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
                     if (!crosses) continue;
                     int qx = lx - dx, qy = ly - dy, qz = lz - dz;
                     if (qx < 0 || qx >= wl || qy < 0 || qy >= hl || qz < 0 || qz >= dl) continue;
-                    connect_s(acc, p, qx + qy * RS + qz * SLICE, MERGE_BOUND_SMEM);
+                    const int qi = qx + qy * RS + qz * SLICE;
+                    if (offs.n > 3) {  // 8/26-connectivity: skip diagonal edges implied by others
+                        const uint32_t kp = W::key(acc.load(p)), kq = W::key(acc.load(qi));
+                        auto key_at = [&](int sx, int sy, int sz) {
+                            return W::key(acc.load(p + sx + sy * RS + sz * SLICE));
+                        };
+                        if (edge_implied(-dx, -dy, -dz, kp < kq ? kp : kq, key_at)) continue;
+                    }
+                    connect_s(acc, p, qi, MERGE_BOUND_SMEM);
                 }
             }
             // levels are ordered for shorter merge walks, not for correctness:

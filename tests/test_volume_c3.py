@@ -10,7 +10,12 @@ dh * volume terms are summed in a different order; non-compactness of 3-D nodes
 divides by pow(volume, 5/3), evaluated to within an ulp of glibc).  The smaller
 volume also covers the operations built from the filter: extract, the differential
 morphological profile and the attribute check.
+
+The 512^3 case needs about 4.5 minutes of single-threaded oracle time and 21 GB of
+host memory, so it runs only with DCF_LARGE_TESTS=1.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -62,4 +67,24 @@ def test_lognormal_volume_against_oracle(ctx, n):
         for i, lam in enumerate(lv[1:]):
             assert np.array_equal(dmp[i], port.filter(17, float(lam), 0, extract=True)), float(lam)
         np.testing.assert_allclose(t.check(17), port.check(17), rtol=1e-6, atol=0)
+    t.close()
+
+
+@pytest.mark.skipif(os.environ.get("DCF_LARGE_TESTS") != "1",
+                    reason="512^3 oracle run: about 4.5 min on one core and 21 GB; set DCF_LARGE_TESTS=1")
+def test_lognormal_volume_512_against_oracle(ctx):
+    n = 512
+    vol = lognormal_volume(n)
+    port = oracle.Port(threads=1)
+    port.load(vol, 6, "max")
+    port.prepare(17)
+    t = ctx.build(vol, connectivity=6, tree_type="max", attribute=17)
+    assert np.array_equal(t.parent(), port.parent())
+    assert np.array_equal(t.filter(17, 2.0, "direct"), port.filter(17, 2.0, 0))
+    assert np.array_equal(t.node_attribute(0), port.node_attr(0), equal_nan=True)
+    np.testing.assert_allclose(t.node_attribute(17), port.node_attr(17), rtol=RTOL, atol=0, equal_nan=True)
+    lv_vol = list(np.geomspace(1.0, float(n) ** 3, 16))
+    spec = t.pattern_spectrum2d(17, dcf.lvec_from_values(LV_NCOMP), 0, dcf.lvec_from_values(lv_vol))
+    want = port.pattern2d(17, LV_NCOMP, 0, lv_vol)
+    np.testing.assert_allclose(spec, want, rtol=RTOL, atol=RTOL * np.abs(want).max())
     t.close()
