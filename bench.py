@@ -401,12 +401,16 @@ def run_batch(args, ctx, stream):
     spec = (13, l_tr, 0, l_ar)
     b = ctx.batch(shapes, np.float32, connectivity=8, attribute=13)
     spectra = torch.empty((len(shapes), l_ar.size, l_tr.size), dtype=torch.float64, device="cuda")
-    # the schedule is tuned on a sample batch (the first tune_n cutouts) and applied
-    # to the whole batch, so that tuning stays within seconds
+    # the schedule is tuned on the batch itself (default), or on a sample batch of the
+    # first tune_n cutouts applied to the whole batch.  A small sample misleads: its
+    # seam merge is bound by the longest chain walks, the whole batch's by contention,
+    # so they prefer different merge orders.
     tune_n = min(len(shapes), args.tune_sample)
     t0 = time.perf_counter()
     tune_ms = None
-    if not args.no_autotune:
+    if not args.no_autotune and tune_n == len(shapes):
+        tune_ms = b.autotune(pix, repeats=1)
+    elif not args.no_autotune:
         tb = ctx.batch(shapes[:tune_n], np.float32, connectivity=8, attribute=13)
         tune_px = sum(h * w for h, w in shapes[:tune_n])
         tune_ms = tb.autotune(pix[:tune_px], repeats=1)
@@ -636,7 +640,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="batched workload: keep the default schedule")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--loop-sample", type=int, default=512, help="cutouts timed through the single-image API")
-    ap.add_argument("--tune-sample", type=int, default=512, help="cutouts the batch schedule is tuned on")
+    ap.add_argument("--tune-sample", type=int, default=4096, help="cutouts the batch schedule is tuned on")
     ap.add_argument("--adj-count", type=int, default=256)
     args = ap.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
