@@ -315,8 +315,9 @@ def run_ours(args):
                      "traffic_source": "ncu DRAM read+write of one 4096^2 launch, scaled by pixels",
                      "share": round(dom_ms / total_prof, 4) if total_prof else None,
                      "alg_bytes_per_launch": alg, "peak_source": f"{peak_kind} hbm_gbs"},
-        "e2e": {"value": round(world * npix / 1e6 / (e2e_ms * 1e-3), 3), "unit": "Mpx/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
+        "e2e": None if args.no_e2e else {
+            "value": round(world * npix / 1e6 / (e2e_ms * 1e-3), 3), "unit": "Mpx/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
