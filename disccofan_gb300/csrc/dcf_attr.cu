@@ -40,12 +40,40 @@ __global__ void k_attr_pixels(const float *__restrict__ gval, Geom g, const int 
         unsigned grp = __match_any_sync(0xffffffffu, node);
         if (valid && lane == __ffs(grp) - 1) atomicAdd(a.area + node, (unsigned)__popc(grp));
         if (G == 0 || !valid) continue;
-        const unsigned x = (unsigned)(p % g.W), y = (unsigned)((p / g.W) % g.H), z = (unsigned)(p / g.WH);
+        // coordinates: one division per warp for its first pixel; lanes add their
+        // offset unless the warp's 32 pixels run past the end of a row
+        const long long zb = base / g.WH, rem = base - zb * g.WH;
+        const long long yb = rem / g.W, xb = rem - yb * g.W;
+        const bool one_row = xb + 31 < g.W;  // warp-uniform
+        unsigned x, y, z;
+        if (one_row) {
+            x = (unsigned)xb + lane;
+            y = (unsigned)yb;
+            z = (unsigned)zb;
+        } else {
+            x = (unsigned)(p % g.W);
+            y = (unsigned)((p / g.W) % g.H);
+            z = (unsigned)(p / g.WH);
+        }
         if (G == 1) {
-            // lanes of one node reduce first; their leader issues the atomics
-            const unsigned mnx = __reduce_min_sync(grp, x), mny = __reduce_min_sync(grp, y);
-            const unsigned mxx = __reduce_max_sync(grp, x + 1), mxy = __reduce_max_sync(grp, y + 1);
-            const unsigned mnz = __reduce_min_sync(grp, z), mxz = __reduce_max_sync(grp, z + 1);
+            // lanes of one node reduce first; their leader issues the atomics.  Within
+            // one row the group's x range is its first and last lane.
+            unsigned mnx, mxx, mny, mxy, mnz, mxz;
+            if (one_row) {
+                mnx = (unsigned)xb + (unsigned)(__ffs(grp) - 1);
+                mxx = (unsigned)xb + (unsigned)(32 - __clz(grp));
+                mny = y;
+                mxy = y + 1;
+                mnz = z;
+                mxz = z + 1;
+            } else {
+                mnx = __reduce_min_sync(grp, x);
+                mny = __reduce_min_sync(grp, y);
+                mxx = __reduce_max_sync(grp, x + 1);
+                mxy = __reduce_max_sync(grp, y + 1);
+                mnz = __reduce_min_sync(grp, z);
+                mxz = __reduce_max_sync(grp, z + 1);
+            }
             if (lane == __ffs(grp) - 1) {
                 atomicMin(a.bmin[0] + node, mnx);
                 atomicMin(a.bmin[1] + node, mny);

@@ -338,44 +338,95 @@ __device__ __forceinline__ int find_scale(const float *lv, int n, double v)
 
 constexpr int SPEC_SMEM_BINS = 4096;
 
+// EXACT: u8/u16 levels and unit pixel sizes, so every dh * area is an integer below
+// 2^48 and every bin's sum is below 2^53 (the sum of all bins is the image's grey
+// sum): any summation order gives the reference's double sums bit for bit.  The
+// lanes of a warp that hit one bin then add their terms first (three 22-bit limbs,
+// one __reduce_add_sync each) and their leader issues one shared-memory 64-bit
+// integer atomic; otherwise every node adds its double term on its own.
+template <bool EXACT>
 __global__ void k_spectrum(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
                            const float *__restrict__ gval, AttrBufs a, int a1, const float *__restrict__ l1, int n1,
                            int a2, const float *__restrict__ l2, int n2, float pd0, float pd1, float pd2,
                            double *spec)
 {
     __shared__ double hist[SPEC_SMEM_BINS];
+    unsigned long long *ihist = (unsigned long long *)hist;
     const int nbins = n1 * n2;
     const bool priv = nbins <= SPEC_SMEM_BINS;
     if (priv)
         for (int i = threadIdx.x; i < nbins; i += blockDim.x) hist[i] = 0.0;
     __syncthreads();
     const float pd[3] = {pd0, pd1, pd2};
-    GRID_LOOP(p, g.N)
-    {
-        if (!isroot[p]) continue;
-        const int q = parent[p];
-        const float dh = q != NONE ? __fsub_rn(gval[p], gval[q]) : gval[p];
-        if (dh == 0.0f) continue;
-        const double ar = area_value(a, (int)p, pd);
-        const int s1 = find_scale(l1, n1, a1 < 0 ? ar : attr_value(a, a1, (int)p, pd));
-        const int s2 = n2 <= 1 ? 0 : find_scale(l2, n2, a2 < 0 ? ar : attr_value(a, a2, (int)p, pd));
-        const double v = (double)dh * ar;
-        if (priv) atomicAdd(hist + s1 + s2 * n1, v);
-        else atomicAdd(spec + s1 + s2 * n1, v);
+    if (EXACT) {
+        const int lane = threadIdx.x & 31;
+        const long long wstride = (long long)gridDim.x * blockDim.x;
+        // whole warps iterate together so the match below sees the full warp
+        for (long long base = (blockIdx.x * (long long)blockDim.x + threadIdx.x) - lane; base < g.N;
+             base += wstride) {
+            const long long p = base + lane;
+            int bin = -1;
+            unsigned long long v = 0;
+            if (p < g.N && isroot[p]) {
+                const int q = parent[p];
+                const float dh = q != NONE ? __fsub_rn(gval[p], gval[q]) : gval[p];
+                if (dh != 0.0f) {
+                    const double ar = area_value(a, (int)p, pd);
+                    const int s1 = find_scale(l1, n1, a1 < 0 ? ar : attr_value(a, a1, (int)p, pd));
+                    const int s2 = n2 <= 1 ? 0 : find_scale(l2, n2, a2 < 0 ? ar : attr_value(a, a2, (int)p, pd));
+                    bin = s1 + s2 * n1;
+                    v = (unsigned long long)((double)dh * ar);
+                }
+            }
+            const unsigned grp = __match_any_sync(0xffffffffu, bin);
+            if (bin < 0) continue;
+            const unsigned long long lo = __reduce_add_sync(grp, (unsigned)(v & 0x3FFFFFu));
+            const unsigned long long mid = __reduce_add_sync(grp, (unsigned)((v >> 22) & 0x3FFFFFu));
+            const unsigned long long hi = __reduce_add_sync(grp, (unsigned)(v >> 44));
+            if (lane != __ffs(grp) - 1) continue;
+            const unsigned long long sum = lo + (mid << 22) + (hi << 44);
+            if (priv) atomicAdd(ihist + bin, sum);
+            else atomicAdd(spec + bin, (double)sum);
+        }
+    } else {
+        GRID_LOOP(p, g.N)
+        {
+            if (!isroot[p]) continue;
+            const int q = parent[p];
+            const float dh = q != NONE ? __fsub_rn(gval[p], gval[q]) : gval[p];
+            if (dh == 0.0f) continue;
+            const double ar = area_value(a, (int)p, pd);
+            const int s1 = find_scale(l1, n1, a1 < 0 ? ar : attr_value(a, a1, (int)p, pd));
+            const int s2 = n2 <= 1 ? 0 : find_scale(l2, n2, a2 < 0 ? ar : attr_value(a, a2, (int)p, pd));
+            const double v = (double)dh * ar;
+            if (priv) atomicAdd(hist + s1 + s2 * n1, v);
+            else atomicAdd(spec + s1 + s2 * n1, v);
+        }
     }
     if (!priv) return;
     __syncthreads();
-    for (int i = threadIdx.x; i < nbins; i += blockDim.x)
-        if (hist[i] != 0.0) atomicAdd(spec + i, hist[i]);
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) {
+        if (EXACT) {
+            if (ihist[i] != 0) atomicAdd(spec + i, (double)ihist[i]);
+        } else if (hist[i] != 0.0) {
+            atomicAdd(spec + i, hist[i]);
+        }
+    }
 }
 
 void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *l1, int n1, int a2, const float *l2,
                      int n2, double *spec, int sm, cudaStream_t s)
 {
     const int nb = grid_for(t.g.N, 256, sm);
+    const bool exact = t.integer_levels && t.pixdim[0] == 1.0f && t.pixdim[1] == 1.0f && t.pixdim[2] == 1.0f;
     prof_begin(P_SPECTRUM, s);
-    k_spectrum<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
-                                  t.pixdim[1], t.pixdim[2], spec); note_launch();
+    if (exact)
+        k_spectrum<true><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
+                                            t.pixdim[1], t.pixdim[2], spec);
+    else
+        k_spectrum<false><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
+                                             t.pixdim[1], t.pixdim[2], spec);
+    note_launch();
     prof_end(P_SPECTRUM, s);
 }
 
