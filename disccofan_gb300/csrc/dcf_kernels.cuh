@@ -31,7 +31,7 @@ inline size_t tile_smem_bytes(int tw, int th, int td, int word_bytes = 8)
 }
 // launch shape of the tile kernels per pixel type: u8/u16 tiles use 32-bit shared
 // words and 128-thread CTAs (25 KB for 64x64: 8 resident per SM), u32/f32 tiles
-// 64-bit words and 256 threads (50 KB: 4 per SM)
+// 64-bit words and 256 threads (42 KB: 5 per SM)
 template <typename T> struct TileCfg {
     static constexpr bool narrow = sizeof(T) <= 2;
     static constexpr int threads = narrow ? TILE_THREADS_NARROW : TILE_THREADS;
