@@ -463,9 +463,12 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
         return set_err(ctx, DCF_ERR_INVALID, "bad attribute %d", attr_idx);
     const uint64_t W = img->dims[0], H = img->dims[1], D = img->dims[2] ? img->dims[2] : 1;
     if (W == 0 || H == 0) return set_err(ctx, DCF_ERR_INVALID, "empty image");
+    // each extent below 2^31, so W * H and then (W * H) * D cannot wrap around 64 bits
+    if (W > 0x7FFFFFFF || H > 0x7FFFFFFF || D > 0x7FFFFFFF || W * H >= 0x7FFFFFFFull ||
+        W * H * D >= 0x7FFFFFFFull)
+        return set_err(ctx, DCF_ERR_INVALID, "image too large (%llu x %llu x %llu; limit 2^31-1 pixels)",
+                       (unsigned long long)W, (unsigned long long)H, (unsigned long long)D);
     const unsigned long long N = W * H * D;
-    if (W > 0x7FFFFFFF || H > 0x7FFFFFFF || D > 0x7FFFFFFF || N >= 0x7FFFFFFFull)
-        return set_err(ctx, DCF_ERR_INVALID, "image too large (%llu pixels; limit 2^31-1)", N);
     int conn = img->connectivity;
     // io.c:64-79
     if (D > 1 && conn == 4) conn = 6;

@@ -210,3 +210,22 @@ def test_bad_arguments(ctx):
         t.filter(0, 1.0, rule=7)
     with pytest.raises(dcf.DcfError):
         t.pattern_spectrum2d(0, dcf.lvec_from_values([1]), 3, dcf.lvec_from_values([1]))
+
+
+def test_oversized_dims_rejected_before_any_copy(ctx):
+    # extents whose product wraps around 64 bits must be refused from the header
+    # alone (the data pointer is a one-byte buffer that must never be read)
+    import ctypes as C
+    buf = np.zeros(1, np.uint8)
+    for dims in ((1 << 22, 1 << 22, 1 << 22), (1 << 31, 1, 1), (70000, 70000, 1)):
+        im = dcf._Image()
+        im.data = buf.ctypes.data
+        im.dtype = 0
+        im.on_device = 0
+        im.dims[:] = list(dims)
+        im.connectivity = 4 if dims[2] == 1 else 6
+        im.tree_type = 0
+        im.pixdim[:] = [1.0, 1.0, 1.0]
+        h = C.c_void_p()
+        assert ctx.lib.dcf_tree_build(ctx.h, C.byref(im), 0, C.byref(h)) == 1, dims
+        assert not h.value
