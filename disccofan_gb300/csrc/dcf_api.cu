@@ -42,7 +42,10 @@ struct dcf_ctx {
     int tile2d[2] = {64, 64};         // build tile of 2-D images (width, height)
     int tile3d[3] = {16, 16, 16};     // build tile of 3-D images
     int level_sync = 1;               // barrier between band-merge levels inside a tile
-    int seam_buckets = 0;             // level buckets of the seam merge (0: every seam edge at once)
+    // level buckets of the seam merge: 1 = every cross-tile edge at once, from a
+    // compacted list (full warps: most face/offset work items hold no edge); 0 = at
+    // once straight from the work items
+    int seam_buckets = 1;
     std::mutex trees_mu;
     std::set<dcf_tree *> trees;       // live trees; orphaned (stream cleared) when the context goes
     DevBuf scratch[16];               // reusable work buffers (filter, spectra, attributes, seams)
