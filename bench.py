@@ -280,11 +280,9 @@ def run_ours(args):
     }
     alg = per_launch.get(dom, npix * s_in)
     # DRAM bytes per pixel per launch from one ncu capture of the kernel on a
-    # 4096^2 uint16 image (profiles/k_tile_build_4096_u16.md,
-    # profiles/k_seam_direct_4096_u16.md), scaled by pixels: traffic grows with
-    # the pixel count for these per-pixel passes
-    dram_per_px = {"tile_build": (33.69472e6 + 154.18496e6) / 4096 ** 2,
-                   "seam_merge": (133.23904e6 + 70.819584e6) / 4096 ** 2}
+    # 4096^2 uint16 image (profiles/k_tile_build_4096_u16.md), scaled by pixels:
+    # traffic grows with the pixel count for this per-pixel pass
+    dram_per_px = {"tile_build": (33.69472e6 + 154.18496e6) / 4096 ** 2}
     traffic = round(dram_per_px[dom] * npix) if dom in dram_per_px else None
     achieved = alg / (dom_ms / dom_n * 1e-3) / 1e9
     B_alg = 2 * (npix * (s_in + 4 + s_in) + 12 * M) + 2 * 8 * 441
