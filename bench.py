@@ -54,6 +54,15 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(values, device):
+    """Element-wise maximum of `values` over the ranks of the default process group
+    (every rank gets it): the job's time is its slowest replica's."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -253,9 +262,7 @@ def run_ours(args):
     d2h = 2 * (npix * 4 + h_spec[0].nbytes)
 
     if world > 1:
-        tt = torch.tensor([ms, e2e_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_ms = float(tt[0]), float(tt[1])
+        ms, e2e_ms = max_over_ranks([ms, e2e_ms], "cuda")
     if rank != 0:
         return None
 
