@@ -174,7 +174,7 @@ def reference_case(ref: oracle.Reference, img: np.ndarray, conn: int, tree: str)
     return out
 
 
-def main(refdir: str = "/root/reference") -> None:
+def main(refdir: str = "/root/reference", outdir: str = HERE) -> None:
     ck = os.path.join(refdir, "tests", "checkimg")
     lena = np.flipud(read_png_gray8(os.path.join(ck, "input_image.png"))).copy()
     gt_area = np.flipud(read_png_gray8(os.path.join(ck, "GT_area_200.png"))).copy()
@@ -208,7 +208,7 @@ def main(refdir: str = "/root/reference") -> None:
     csl_lena = lref.csl(0, lvec_txt)
     del lref
     np.savez_compressed(
-        os.path.join(HERE, "lena_fixtures.npz"),
+        os.path.join(outdir, "lena_fixtures.npz"),
         lena=lena, gt_area_200=gt_area, gt_ncomp_0_2=gt_ncomp,
         check_area_c4=chk_area, check_area_c8=chk_area8, check_ncomp_c4=chk_ncomp,
         tree_index=np.array(idx, np.int64), tree_parent=np.array(par, np.int64),
@@ -231,8 +231,8 @@ def main(refdir: str = "/root/reference") -> None:
         res = reference_case(ref, img, conn, tree)
         for k, v in res.items():
             cases[f"{name}/{k}"] = v
-    np.savez_compressed(os.path.join(HERE, "synthetic_reference.npz"), **cases)
-    print("wrote", os.path.join(HERE, "lena_fixtures.npz"), "and synthetic_reference.npz")
+    np.savez_compressed(os.path.join(outdir, "synthetic_reference.npz"), **cases)
+    print("wrote", os.path.join(outdir, "lena_fixtures.npz"), "and synthetic_reference.npz")
 
 
 if __name__ == "__main__":

@@ -9,6 +9,7 @@ import pytest
 from oracle import oracle
 
 REF_SRC = "/root/reference/src/sources/flood.c"
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def test_port_lena_filters(port_lib, lena):
@@ -118,3 +119,21 @@ def test_port_matches_compiled_reference_random():
         assert np.array_equal(ref.parent(), port.parent())
         assert np.array_equal(ref.pattern2d(16, [0.9, 1.1, 1.5], 0, [3, 9, 27]),
                               port.pattern2d(16, [0.9, 1.1, 1.5], 0, [3, 9, 27]))
+
+
+@pytest.mark.reference
+def test_golden_fixtures_regenerate_identically(tmp_path):
+    # the committed fixtures are exactly what tests/golden/make_golden.py makes from
+    # the reference checkout and the reference compiled from it
+    if not os.path.exists(REF_SRC):
+        pytest.skip("reference checkout absent")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    mg.main(os.path.dirname(os.path.dirname(os.path.dirname(REF_SRC))), str(tmp_path))
+    for name in ("lena_fixtures.npz", "synthetic_reference.npz"):
+        want, got = np.load(os.path.join(GOLDEN, name)), np.load(str(tmp_path / name))
+        assert sorted(want.files) == sorted(got.files), name
+        for k in want.files:
+            assert np.array_equal(want[k], got[k], equal_nan=want[k].dtype.kind == "f"), (name, k)
