@@ -114,6 +114,7 @@ def library() -> C.CDLL:
         "dcf_tree_export": [vp, vp, i, C.c_char_p],
         "dcf_csl": [vp, vp, i, vp, i, vp, vp, vp, i],
         "dcf_fits_read": [C.c_char_p, vp, u64, C.POINTER(u64 * 3), C.POINTER(i)],
+        "dcf_fits_read_raw": [C.c_char_p, vp, u64, C.POINTER(u64 * 3), C.POINTER(i)],
         "dcf_batch_create": [vp, i, vp, vp, i, i, i, vp, C.POINTER(vp)],
         "dcf_batch_destroy": [vp],
         "dcf_batch_info": [vp, C.POINTER(u64), C.POINTER(u64), vp, C.POINTER(u64)],
@@ -185,6 +186,24 @@ def read_fits(path: str) -> np.ndarray:
     w, h, d = dims[0], dims[1], dims[2]
     out = np.empty(w * h * d, np.float32)
     st = L.dcf_fits_read(path.encode(), out.ctypes.data, out.size, C.byref(dims), C.byref(bp))
+    if st:
+        raise DcfError(st, path)
+    return out.reshape((h, w) if d == 1 else (d, h, w))
+
+
+def read_fits_raw(path: str) -> np.ndarray:
+    """Primary FITS image in its own pixel type (uint8, uint16 with BZERO 32768,
+    uint32 with BZERO 2^31, float32), for a build without a float copy; raises
+    DcfError (status unsupported) for other scalings, which read_fits handles."""
+    L = library()
+    dims = (C.c_uint64 * 3)()
+    dt = C.c_int()
+    st = L.dcf_fits_read_raw(path.encode(), None, 0, C.byref(dims), C.byref(dt))
+    if st:
+        raise DcfError(st, path)
+    w, h, d = dims[0], dims[1], dims[2]
+    out = np.empty(w * h * d, (np.uint8, np.uint16, np.uint32, np.float32)[dt.value])
+    st = L.dcf_fits_read_raw(path.encode(), out.ctypes.data, out.nbytes, C.byref(dims), C.byref(dt))
     if st:
         raise DcfError(st, path)
     return out.reshape((h, w) if d == 1 else (d, h, w))

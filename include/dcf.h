@@ -30,6 +30,7 @@
  *   dcf_lvec_read             lambda_vector_read              src/sources/lambdavec.c:35
  *   dcf_tree_export           write_tree                      src/sources/io.c:1431
  *   dcf_fits_read             the FITS branch of the tile reader src/sources/io.c:624-706
+ *   dcf_fits_read_raw         (same, in the file's own pixel type)
  *   dcf_batch_*               (no reference counterpart: many cutouts per launch)
  *   dcf_adjoint_*             (no reference counterpart: gradients for float images)
  */
@@ -242,6 +243,12 @@ dcf_status dcf_tree_export(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, const cha
  * axis lengths (1 for missing axes), *bitpix the file's BITPIX; out == NULL reads
  * the header only; capacity (in pixels) must cover dims[0]*dims[1]*dims[2]. */
 dcf_status dcf_fits_read(const char *path, float *out, uint64_t capacity, uint64_t dims[3], int *bitpix);
+/* The same image in its own pixel type, to pass to dcf_tree_build without a float
+ * copy (for C2/C3-scale inputs): BITPIX 8 -> DCF_U8, BITPIX 16 with BZERO 32768 ->
+ * DCF_U16, BITPIX 32 with BZERO 2147483648 -> DCF_U32, BITPIX -32 -> DCF_F32, all
+ * with BSCALE 1 (else DCF_ERR_UNSUPPORTED: use dcf_fits_read).  *dtype receives the
+ * dcf_dtype; out == NULL reads the header only; capacity_bytes must cover the data. */
+dcf_status dcf_fits_read_raw(const char *path, void *out, uint64_t capacity_bytes, uint64_t dims[3], int *dtype);
 
 /* ---- lambda vectors ---- */
 /* Read a "#LambdaVector file..." file: out[0] = 0, out[i] = value_i / imscale.

@@ -72,3 +72,41 @@ def test_fits_reads_reference_fixtures(lena):
     for name, key in (("GT_2D_check_area.fits", "check_area_c4"), ("GT_2D_check_area_8.fits", "check_area_c8"),
                       ("GT_2D_check_ncomp.fits", "check_ncomp_c4")):
         assert np.array_equal(dcf.read_fits(os.path.join(REF_CHECKIMG, name)), lena[key]), name
+
+
+@pytest.mark.parametrize("kind", ["u8", "u16", "u32", "f32"])
+def test_fits_raw_matches_float_read(tmp_path, kind):
+    # the raw read gives the file's unsigned / float pixels, equal to the float read
+    # once converted (u32 with the same round-to-nearest as the tree build)
+    rng = np.random.default_rng(len(kind) + ord(kind[1]))
+    shape = (2, 9, 11) if kind == "u32" else (19, 23)
+    if kind == "u8":
+        want, bitpix, bzero, stored = rng.integers(0, 256, shape).astype(np.uint8), 8, None, None
+    elif kind == "u16":
+        want, bitpix, bzero = rng.integers(0, 65536, shape).astype(np.uint16), 16, 32768.0
+        stored = want.astype(np.int64) - 32768
+    elif kind == "u32":
+        want, bitpix, bzero = rng.integers(0, 2**32, shape, dtype=np.uint64).astype(np.uint32), 32, 2147483648.0
+        stored = want.astype(np.int64) - 2**31
+    else:
+        want, bitpix, bzero, stored = rng.standard_normal(shape).astype(np.float32), -32, None, None
+    p = str(tmp_path / f"raw_{kind}.fits")
+    write_fits(p, want if stored is None else stored, bitpix, bzero)
+    got = dcf.read_fits_raw(p)
+    assert got.dtype == want.dtype and got.shape == shape
+    assert np.array_equal(got, want)
+    assert np.array_equal(got.astype(np.float32), dcf.read_fits(p))
+
+
+def test_fits_raw_refuses_other_scalings(tmp_path):
+    p = str(tmp_path / "signed16.fits")
+    write_fits(p, np.arange(-6, 6).reshape(3, 4), 16)        # signed 16-bit: no BZERO
+    with pytest.raises(dcf.DcfError) as e:
+        dcf.read_fits_raw(p)
+    assert e.value.status == 8
+    q = str(tmp_path / "scaled.fits")
+    write_fits(q, np.arange(12).reshape(3, 4), 8, bscale=2.0)
+    with pytest.raises(dcf.DcfError) as e:
+        dcf.read_fits_raw(q)
+    assert e.value.status == 8
+    assert np.array_equal(dcf.read_fits(q), 2.0 * np.arange(12, dtype=np.float32).reshape(3, 4))
