@@ -392,6 +392,44 @@ def make_cutouts(count: int = 4096, seed: int = 4, device="cuda"):
     return [(int(h), int(w)) for h, w in zip(hs, ws)], pix
 
 
+def batch_cpu_baseline(shapes, pix, count: int, threads: int | None = None):
+    """The batched workload on the host: the oracle on the first `count` cutouts,
+    timed two ways -- one cutout at a time on all host threads, and the cutouts
+    spread over the host threads with one thread each -- and the faster reported."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle
+    oracle.build(ref=False)
+    threads = threads or os.cpu_count() or 1
+    l_tr = list(np.geomspace(1, 1e11, 24))
+    l_ar = list(np.geomspace(1, 1 << 20, 24))
+    npx = sum(h * w for h, w in shapes[:count])
+    host = pix[:npx].to("cpu").numpy()
+    views, o = [], 0
+    for h, w in shapes[:count]:
+        views.append(host[o:o + h * w].reshape(h, w))
+        o += h * w
+
+    def one(v, nt):
+        p = oracle.Port(threads=nt)
+        p.load(v, 8, "max", threads=nt)
+        p.pattern2d(13, l_tr, 0, l_ar)
+        del p
+
+    t0 = time.perf_counter()
+    for v in views:
+        one(v, threads)
+    t_all = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:  # the oracle's C calls release the GIL
+        list(ex.map(lambda v: one(v, 1), views))
+    t_spread = time.perf_counter() - t0
+    best = min(t_all, t_spread)
+    return {"value": round(npx / 1e6 / best, 3), "unit": "Mpx/s", "cores": threads, "kind": "port",
+            "sample": f"first {count} cutouts ({npx} px), max-tree 8-conn, inertia group, 2D spectrum; one "
+                      f"cutout at a time on {threads} threads {t_all:.2f} s, cutouts over {threads} threads "
+                      f"one each {t_spread:.2f} s; the faster"}
+
+
 def run_batch(args, ctx, stream):
     """The batched workload: 4096 float32 cutouts (64..1024 a side), max-tree 8-conn,
     inertia group, 2-D spectrum inertia trace (13) x area (0) on 24 log thresholds each
@@ -479,7 +517,8 @@ def run_batch(args, ctx, stream):
             "schedule": {"tile": info["tile"], "ctas_per_sm": info["ctas_per_sm"], "chunk": info["chunk"]},
             "autotune": {"sample_cutouts": tune_n, "best_sample_build_ms": None if tune_ms is None else round(tune_ms, 3),
                          "seconds": round(tune_s, 2), "seam_buckets": info["seam_buckets"], "up_steps": info["up_steps"]},
-            "graph_kernels": info["graph_kernels"], "gpu_launches_per_step": int(graph_launches), "steps": steps}
+            "graph_kernels": info["graph_kernels"], "gpu_launches_per_step": int(graph_launches), "steps": steps,
+            "cpu_baseline": None if args.no_cpu else batch_cpu_baseline(shapes, pix, args.batch_cpu_sample)}
 
 
 # ---------------------------------------------------------------------------
@@ -648,6 +687,7 @@ def main():
     ap.add_argument("--loop-sample", type=int, default=512, help="cutouts timed through the single-image API")
     ap.add_argument("--tune-sample", type=int, default=4096, help="cutouts the batch schedule is tuned on")
     ap.add_argument("--adj-count", type=int, default=256)
+    ap.add_argument("--batch-cpu-sample", type=int, default=64, help="cutouts of the batch's CPU baseline")
     args = ap.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
     if res is not None:
