@@ -392,6 +392,16 @@ def make_cutouts(count: int = 4096, seed: int = 4, device="cuda"):
     return [(int(h), int(w)) for h, w in zip(hs, ws)], pix
 
 
+def guarded(fn, *a):
+    """A host-side baseline must not cost the run its bench line: a failure is
+    reported in place of the figure."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001 -- reported, not hidden
+        log(f"{fn.__name__} failed: {e!r}")
+        return {"error": repr(e)}
+
+
 def batch_cpu_baseline(shapes, pix, count: int, threads: int | None = None):
     """The batched workload on the host: the oracle on the first `count` cutouts,
     timed two ways -- one cutout at a time on all host threads, and the cutouts
@@ -518,7 +528,7 @@ def run_batch(args, ctx, stream):
             "autotune": {"sample_cutouts": tune_n, "best_sample_build_ms": None if tune_ms is None else round(tune_ms, 3),
                          "seconds": round(tune_s, 2), "seam_buckets": info["seam_buckets"], "up_steps": info["up_steps"]},
             "graph_kernels": info["graph_kernels"], "gpu_launches_per_step": int(graph_launches), "steps": steps,
-            "cpu_baseline": None if args.no_cpu else batch_cpu_baseline(shapes, pix, args.batch_cpu_sample)}
+            "cpu_baseline": None if args.no_cpu else guarded(batch_cpu_baseline, shapes, pix, args.batch_cpu_sample)}
 
 
 # ---------------------------------------------------------------------------
