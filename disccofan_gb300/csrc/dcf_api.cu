@@ -46,6 +46,15 @@ struct dcf_ctx {
     // compacted list (full warps: most face/offset work items hold no edge); 0 = at
     // once straight from the work items
     int seam_buckets = 1;
+    // Test knobs, read from the environment at creation.  merge_bound (DCF_MERGE_BOUND):
+    // iteration limit of every tree-merge loop (0 = the built-in limits); a small
+    // value makes merges give up, which must surface as DCF_ERR_TIMEOUT.
+    // fail_alloc (DCF_FAIL_ALLOC = k): the k-th device allocation made through this
+    // context (counting from 0) reports out-of-memory without allocating, which must
+    // surface as DCF_ERR_NOMEM with nothing leaked; -1 = off.
+    long long merge_bound = 0;
+    long long fail_alloc = -1;
+    long long allocs = 0;
     std::mutex trees_mu;
     std::set<dcf_tree *> trees;       // live trees; orphaned (stream cleared) when the context goes
     DevBuf scratch[16];               // reusable work buffers (filter, spectra, attributes, seams)
@@ -144,6 +153,26 @@ static dcf_status set_err(dcf_ctx *c, dcf_status s, const char *fmt, ...)
     return s;
 }
 
+// Every device allocation of the library goes through these two, so that the
+// allocation-failure knob (dcf_ctx::fail_alloc) reaches each of them.
+static bool alloc_refused(dcf_ctx *c)
+{
+    if (!c) return false;
+    return c->allocs++ == c->fail_alloc;
+}
+template <typename T>
+static cudaError_t dmalloc(dcf_ctx *c, T **p, size_t bytes)
+{
+    if (alloc_refused(c)) return cudaErrorMemoryAllocation;
+    return cudaMalloc((void **)p, bytes);
+}
+template <typename T>
+static cudaError_t dmalloc_async(dcf_ctx *c, T **p, size_t bytes, cudaStream_t s)
+{
+    if (alloc_refused(c)) return cudaErrorMemoryAllocation;
+    return cudaMallocAsync((void **)p, bytes, s);
+}
+
 #define CU(call)                                                                                          \
     do {                                                                                                  \
         cudaError_t _e = (call);                                                                          \
@@ -178,7 +207,7 @@ static dcf_status scratch(dcf_ctx *ctx, int slot, size_t bytes, void **out)
         if (b.p) CU(cudaFree(b.p));
         b.p = nullptr;
         b.bytes = 0;
-        CU(cudaMalloc(&b.p, bytes));
+        CU(dmalloc(ctx, &b.p, bytes));
         b.bytes = bytes;
     }
     *out = b.p;
@@ -252,6 +281,11 @@ dcf_status dcf_ctx_create(int device, void *cuda_stream, dcf_ctx **out)
         int v = atoi(e);
         if (v >= 0 && v <= 1024) ctx->seam_buckets = v;
     }
+    if (const char *e = getenv("DCF_MERGE_BOUND")) {
+        long long v = atoll(e);
+        if (v > 0) ctx->merge_bound = v;
+    }
+    if (const char *e = getenv("DCF_FAIL_ALLOC")) ctx->fail_alloc = atoll(e);
     if (const char *e = getenv("DCF_UP_STEPS")) {
         int v = atoi(e);
         if (v >= 0 && v < (1 << 20)) ctx->up_steps = v;
@@ -431,7 +465,7 @@ static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx, bo
     }
     free_attr(t);
     const size_t N = (size_t)t->g.N;
-    CU(cudaMallocAsync(&t->attr_mem, attr_bytes(group, N), ctx->stream));
+    CU(dmalloc_async(ctx, &t->attr_mem, attr_bytes(group, N), ctx->stream));
     AttrBufs &a = t->attr;
     attr_carve(a, group, t->dtype == U8 || t->dtype == U16, t->g.D > 1, N, t->attr_mem);
     if (need_grey) a.grey = true;
@@ -495,6 +529,7 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
     t->g.N = (long long)N;
     t->g.conn = conn;
     t->g.level_sync = ctx->level_sync;
+    t->g.merge_bound = ctx->merge_bound;
     if (D > 1) {
         t->g.tw = ctx->tile3d[0];
         t->g.th = ctx->tile3d[1];
@@ -522,13 +557,13 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
             goto fail;                  \
         }                               \
     } while (0)
-    TRY(cudaMallocAsync(&t->gval, N * sizeof(float), ctx->stream));
-    TRY(cudaMallocAsync(&t->parent, N * sizeof(int), ctx->stream));
-    TRY(cudaMallocAsync(&t->isroot, N, ctx->stream));
-    TRY(cudaMallocAsync(&t->stats, 4 * sizeof(unsigned) + sizeof(unsigned long long), ctx->stream));
+    TRY(dmalloc_async(ctx, &t->gval, N * sizeof(float), ctx->stream));
+    TRY(dmalloc_async(ctx, &t->parent, N * sizeof(int), ctx->stream));
+    TRY(dmalloc_async(ctx, &t->isroot, N, ctx->stream));
+    TRY(dmalloc_async(ctx, &t->stats, 4 * sizeof(unsigned) + sizeof(unsigned long long), ctx->stream));
     t->num_nodes = (unsigned long long *)(t->stats + 4);
     if (!img->on_device) {
-        TRY(cudaMallocAsync(&tmp_in, in_bytes, ctx->stream));
+        TRY(dmalloc_async(ctx, &tmp_in, in_bytes, ctx->stream));
         TRY(cudaMemcpyAsync(tmp_in, img->data, in_bytes, cudaMemcpyHostToDevice, ctx->stream));
         d_in = tmp_in;
     }
@@ -1002,6 +1037,10 @@ extern "C" dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *t, int a
                                                 int extract, float *out_device)
 {
     if (!ctx || !t || !out_device) return DCF_ERR_INVALID;
+    // the fixed array belongs to one device: a tree of another context's device
+    // would be filtered in the wrong device's memory
+    if (!t->ctx || t->ctx->device != ctx->device)
+        return set_err(ctx, DCF_ERR_INVALID, "dcf_filter_direct_noalloc: tree was built on another device");
     if (t->g.N > NOALLOC_MAX_PIXELS)
         return set_err(ctx, DCF_ERR_INVALID, "dcf_filter_direct_noalloc: %lld pixels exceed the fixed scratch of %lld",
                        (long long)t->g.N, NOALLOC_MAX_PIXELS);
@@ -1014,9 +1053,13 @@ extern "C" dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *t, int a
         // name g_noalloc_scratch is not a device address, so look the address up
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
         if (!g_noalloc_ptr[ctx->device]) {
+            // the caller's current device is put back afterwards
+            int prev = -1;
+            CU(cudaGetDevice(&prev));
             CU(cudaSetDevice(ctx->device));
             void *p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            cudaSetDevice(prev);
             if (e != cudaSuccess || !p)
                 return set_err(ctx, DCF_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch): %s", cudaGetErrorString(e));
             g_noalloc_ptr[ctx->device] = p;
@@ -1077,6 +1120,7 @@ struct dcf_batch {
     int tw = 64, th = 64, ctas = 1, chunk = 1;
     int seam_buckets = 16;                   // level buckets of the seam merge (0: all edges at once)
     int up_steps = 2048;                     // bottom-up fold steps per walker
+    long long merge_bound = 0;               // the context's merge-loop limit (test knob)
     int ntiles = 0;
     size_t tiles_cap = 0;
     BatchTile *d_tiles = nullptr;
@@ -1145,6 +1189,7 @@ static TreeView batch_view(const dcf_batch *b)
     v.g.th = b->th;
     v.g.td = 1;
     v.g.level_sync = 1;
+    v.g.merge_bound = b->merge_bound;
     v.tree_min = false;
     v.kmax = b->d_misc + 3;
     v.gval = b->gval;
@@ -1174,7 +1219,7 @@ static dcf_status batch_set_tiles(dcf_ctx *ctx, dcf_batch *b, int tw, int th, in
         if (b->d_tiles) CU(cudaFree(b->d_tiles));
         b->d_tiles = nullptr;
         b->tiles_cap = 0;
-        CU(cudaMalloc(&b->d_tiles, tl.size() * sizeof(BatchTile)));
+        CU(dmalloc(ctx, &b->d_tiles, tl.size() * sizeof(BatchTile)));
         b->tiles_cap = tl.size();
     }
     CU(cudaMemcpyAsync(b->d_tiles, tl.data(), tl.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, ctx->stream));
@@ -1191,7 +1236,7 @@ static dcf_status batch_set_tiles(dcf_ctx *ctx, dcf_batch *b, int tw, int th, in
             if (b->seam_mem) CU(cudaFree(b->seam_mem));
             b->seam_mem = nullptr;
             b->seam_bytes = 0;
-            CU(cudaMalloc(&b->seam_mem, need));
+            CU(dmalloc(ctx, &b->seam_mem, need));
             b->seam_bytes = need;
         }
         // laid out for the largest bucket count, so set_merge can change it in place
@@ -1216,7 +1261,7 @@ static dcf_status batch_ensure_rest(dcf_ctx *ctx, dcf_batch *b, unsigned R)
     if (b->rest_mem) CU(cudaFree(b->rest_mem));
     b->rest_mem = nullptr;
     b->rest_bytes = 0;
-    CU(cudaMalloc(&b->rest_mem, need));
+    CU(dmalloc(ctx, &b->rest_mem, need));
     b->rest_bytes = need;
     return DCF_OK;
 }
@@ -1326,6 +1371,7 @@ dcf_status dcf_batch_create(dcf_ctx *ctx, int count, const uint32_t *widths, con
     dcf_batch *b = new (std::nothrow) dcf_batch();
     if (!b) return DCF_ERR_NOMEM;
     b->ctx = ctx;
+    b->merge_bound = ctx->merge_bound;
     b->count = count;
     b->dtype = dtype;
     b->conn = connectivity;
@@ -1362,16 +1408,16 @@ dcf_status dcf_batch_create(dcf_ctx *ctx, int count, const uint32_t *widths, con
             goto fail;                                                                                        \
         }                                                                                                     \
     } while (0)
-    BTRY(cudaMalloc(&b->d_imgs, count * sizeof(BatchImg)));
-    BTRY(cudaMalloc(&b->d_offs, count * sizeof(long long)));
-    BTRY(cudaMalloc(&b->d_misc, 8 * sizeof(unsigned) + sizeof(unsigned long long)));
+    BTRY(dmalloc(ctx, &b->d_imgs, count * sizeof(BatchImg)));
+    BTRY(dmalloc(ctx, &b->d_offs, count * sizeof(long long)));
+    BTRY(dmalloc(ctx, &b->d_misc, 8 * sizeof(unsigned) + sizeof(unsigned long long)));
     b->d_nodes = (unsigned long long *)(b->d_misc + 8);
-    BTRY(cudaMalloc(&b->pixels, (size_t)N * esize[dtype]));
-    BTRY(cudaMalloc(&b->gval, (size_t)N * 4));
-    BTRY(cudaMalloc(&b->node, (size_t)N * 8));
-    BTRY(cudaMalloc(&b->parent, (size_t)N * 4));
-    BTRY(cudaMalloc(&b->isroot, (size_t)N));
-    BTRY(cudaMalloc(&b->attr_mem, attr_bytes(b->group, (size_t)N)));
+    BTRY(dmalloc(ctx, &b->pixels, (size_t)N * esize[dtype]));
+    BTRY(dmalloc(ctx, &b->gval, (size_t)N * 4));
+    BTRY(dmalloc(ctx, &b->node, (size_t)N * 8));
+    BTRY(dmalloc(ctx, &b->parent, (size_t)N * 4));
+    BTRY(dmalloc(ctx, &b->isroot, (size_t)N));
+    BTRY(dmalloc(ctx, &b->attr_mem, attr_bytes(b->group, (size_t)N)));
     attr_carve(b->attr, b->group, dtype == U8 || dtype == U16, false, (size_t)N, b->attr_mem);
     BTRY(cudaMemcpy(b->d_imgs, b->imgs.data(), count * sizeof(BatchImg), cudaMemcpyHostToDevice));
     BTRY(cudaMemcpy(b->d_offs, offs.data(), count * sizeof(long long), cudaMemcpyHostToDevice));
@@ -1588,17 +1634,17 @@ dcf_status dcf_batch_run(dcf_ctx *ctx, dcf_batch *b, const void *pixels, int pix
     cudaStream_t s = ctx->stream;
     // buffers the requested operations need (allocated once)
     if (o.filter_attr >= 0 && !b->flag) {
-        CU(cudaMalloc(&b->flag, N));
-        CU(cudaMalloc(&b->target, N * 4));
+        CU(dmalloc(ctx, &b->flag, N));
+        CU(dmalloc(ctx, &b->target, N * 4));
     }
-    if (filtered && !outputs_on_device && !b->filtered) CU(cudaMalloc(&b->filtered, N * 4));
+    if (filtered && !outputs_on_device && !b->filtered) CU(dmalloc(ctx, &b->filtered, N * 4));
     const size_t nspec = o.spec_attr1 >= 0 ? (size_t)b->count * o.n1 * o.n2 : 0;
     if (spectra && nspec && !outputs_on_device && nspec > b->spectra_cap) {
         batch_drop_graph(b);
         if (b->spectra) CU(cudaFree(b->spectra));
         b->spectra = nullptr;
         b->spectra_cap = 0;
-        CU(cudaMalloc(&b->spectra, nspec * 8));
+        CU(dmalloc(ctx, &b->spectra, nspec * 8));
         b->spectra_cap = nspec;
     }
     if (o.spec_attr1 >= 0) {
@@ -1607,7 +1653,7 @@ dcf_status dcf_batch_run(dcf_ctx *ctx, dcf_batch *b, const void *pixels, int pix
             if (b->lvec) CU(cudaFree(b->lvec));
             b->lvec = nullptr;
             b->lvec_cap = 0;
-            CU(cudaMalloc(&b->lvec, (size_t)(o.n1 + o.n2) * 4));
+            CU(dmalloc(ctx, &b->lvec, (size_t)(o.n1 + o.n2) * 4));
             b->lvec_cap = o.n1 + o.n2;
         }
         CU(cudaMemcpyAsync(b->lvec, o.lvec1, (size_t)o.n1 * 4, cudaMemcpyHostToDevice, s));
@@ -1781,12 +1827,12 @@ dcf_status dcf_batch_adjoint(dcf_ctx *ctx, dcf_batch *b, const float *grad_filte
     const size_t N = (size_t)b->N;
     const size_t nspec = (size_t)b->count * o.n1 * o.n2;
     cudaStream_t s = ctx->stream;
-    if (!b->adj_acc) CU(cudaMalloc(&b->adj_acc, N * 8));
+    if (!b->adj_acc) CU(dmalloc(ctx, &b->adj_acc, N * 8));
     const float *v = grad_filtered;
     const double *w = grad_spectra;
     float *grad = grad_pixels;
     if (!on_device) {
-        if (!b->adj_io) CU(cudaMalloc(&b->adj_io, N * 8));
+        if (!b->adj_io) CU(dmalloc(ctx, &b->adj_io, N * 8));
         if (grad_filtered) {
             CU(cudaMemcpyAsync(b->adj_io, grad_filtered, N * 4, cudaMemcpyHostToDevice, s));
             v = b->adj_io;
@@ -1796,7 +1842,7 @@ dcf_status dcf_batch_adjoint(dcf_ctx *ctx, dcf_batch *b, const float *grad_filte
                 if (b->adj_w) CU(cudaFree(b->adj_w));
                 b->adj_w = nullptr;
                 b->adj_w_cap = 0;
-                CU(cudaMalloc(&b->adj_w, nspec * 8));
+                CU(dmalloc(ctx, &b->adj_w, nspec * 8));
                 b->adj_w_cap = nspec;
             }
             CU(cudaMemcpyAsync(b->adj_w, grad_spectra, nspec * 8, cudaMemcpyHostToDevice, s));

@@ -106,7 +106,7 @@ __global__ void k_batch_seam(unsigned long long *gnode, Geom bg, const BatchImg 
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
          w += (long long)gridDim.x * blockDim.x) {
         int p, q;
-        if (batch_seam_item(bg, imgs, tiles, offs, fmax, w, gnode, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
+        if (batch_seam_item(bg, imgs, tiles, offs, fmax, w, gnode, p, q)) connect(acc, p, q, merge_bound_global(bg));
     }
 }
 
@@ -303,7 +303,7 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
         cudaMemsetAsync(seam.count, 0, 4, s);
         cudaMemsetAsync(seam.hist, 0, 4 * SEAM_BINS, s);
         k_batch_seam_collect<<<grid_for(work, 256, sm), 256, 0, s>>>(node, bg, imgs, tiles, ntiles, seam); note_launch();
-        launch_seam_buckets(seam, node, bg.N, err, sm, s);
+        launch_seam_buckets(seam, node, bg.N, bg.merge_bound, err, sm, s);
     } else {
         k_batch_seam<<<grid_for(work, 128, sm), 128, 0, s>>>(node, bg, imgs, tiles, ntiles, err); note_launch();
     }

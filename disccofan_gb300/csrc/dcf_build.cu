@@ -132,7 +132,7 @@ __global__ void k_seam_direct(unsigned long long *gnode, Geom g, int ntx, int nt
     for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
          w += (long long)gridDim.x * blockDim.x) {
         int p, q;
-        if (seam_item(g, ntx, nty, offs, fmax, w, gnode, p, q)) connect(acc, p, q, MERGE_BOUND_GLOBAL);
+        if (seam_item(g, ntx, nty, offs, fmax, w, gnode, p, q)) connect(acc, p, q, merge_bound_global(g));
     }
 }
 
@@ -257,24 +257,26 @@ __global__ void k_seam_scatter(SeamEdges e)
     }
 }
 
-__global__ void k_seam_bucket(SeamEdges e, int b, unsigned long long *gnode, long long n, unsigned *err)
+__global__ void k_seam_bucket(SeamEdges e, int b, unsigned long long *gnode, long long n, long long bound,
+                              unsigned *err)
 {
     GlobalAcc acc{gnode, err, n};
     const unsigned lo = e.bstart[b], hi = e.bstart[b + 1];
     for (long long i = lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < hi;
          i += (long long)gridDim.x * blockDim.x) {
         const int2 pq = e.sorted[i];
-        connect(acc, pq.x, pq.y, MERGE_BOUND_GLOBAL);
+        connect(acc, pq.x, pq.y, bound);
     }
 }
 
-void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, unsigned *err, int sm, cudaStream_t s)
+void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, long long merge_bound, unsigned *err,
+                         int sm, cudaStream_t s)
 {
     k_seam_bounds<<<1, 1024, 0, s>>>(e); note_launch();
     k_seam_scatter<<<grid_for(e.cap, 256, sm), 256, 0, s>>>(e); note_launch();
     const int gb = grid_for(e.cap / e.buckets + 1, 128, sm);
     for (int b = 0; b < e.buckets; b++) {
-        k_seam_bucket<<<gb, 128, 0, s>>>(e, b, node, n, err);
+        k_seam_bucket<<<gb, 128, 0, s>>>(e, b, node, n, merge_bound > 0 ? merge_bound : MERGE_BOUND_GLOBAL, err);
         note_launch();
     }
 }
@@ -334,7 +336,7 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
             cudaMemsetAsync(e.count, 0, 4, s);
             cudaMemsetAsync(e.hist, 0, 4 * SEAM_BINS, s);
             k_seam_collect<<<grid_for(work, 256, a.sm_count), 256, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, e); note_launch();
-            launch_seam_buckets(e, a.node, a.g.N, a.err, a.sm_count, s);
+            launch_seam_buckets(e, a.node, a.g.N, a.g.merge_bound, a.err, a.sm_count, s);
         } else {
             k_seam_direct<<<grid_for(work, 128, a.sm_count), 128, 0, s>>>(a.node, a.g, grid.x, grid.y, grid.z, a.err); note_launch();
         }

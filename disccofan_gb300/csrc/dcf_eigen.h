@@ -15,6 +15,19 @@
  *
  * Only IEEE + - * / and sqrt are used.  Build device code with --fmad=false and
  * host code with -ffp-contract=off so no fused multiply-add changes a rounding.
+ *
+ * Provenance and licence.  The value path below (dcf_pythag, dcf_tred2_values,
+ * dcf_tql2_values) follows the operation order, and keeps the variable names, of the
+ * routines PYTHAG, TRED2 and TQL2 of the C port of EISPACK that the reference
+ * vendors (src/sources/eispack.c, functions pythag, tred2 and tql2):
+ *
+ *   Original FORTRAN77 version by Smith, Boyle, Dongarra, Garbow, Ikebe, Klema,
+ *   Moler.  C version by John Burkardt.  That code is distributed under the GNU
+ *   LGPL license.
+ *
+ * Being a transcription of that code's arithmetic, this file is likewise
+ * distributed under the GNU Lesser General Public License; the rest of the library
+ * only calls it.
  */
 #ifndef DCF_EIGEN_H
 #define DCF_EIGEN_H

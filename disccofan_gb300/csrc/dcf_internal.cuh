@@ -38,6 +38,7 @@ struct Geom {
     int conn;
     int tw, th, td;  // build tile extents (tw*th*td <= 4096)
     int level_sync;  // barrier between the band-merge levels of a tile
+    long long merge_bound;  // iteration limit of the merge loops (0: the built-in limits)
 };
 
 // Grey level as the reference holds it (types.h:53 `value` = float): the pixel

@@ -22,6 +22,14 @@ constexpr int TILE_THREADS_NARROW = 128; // with 32-bit words (u8/u16): more til
 constexpr int TILE_MAX_PIX = 4096;             // largest build tile (16-bit local indices)
 constexpr long long MERGE_BOUND_SMEM = 1LL << 22;
 constexpr long long MERGE_BOUND_GLOBAL = 1LL << 28;
+__host__ __device__ inline long long merge_bound_smem(const Geom &g)
+{
+    return g.merge_bound > 0 ? g.merge_bound : MERGE_BOUND_SMEM;
+}
+__host__ __device__ inline long long merge_bound_global(const Geom &g)
+{
+    return g.merge_bound > 0 ? g.merge_bound : MERGE_BOUND_GLOBAL;
+}
 
 // dynamic shared memory of one tile build (padded node words + padded row stacks);
 // word_bytes 8 (u32/f32 images) or 4 (u8/u16: 16-bit level and parent)
@@ -73,8 +81,8 @@ size_t seam_edges_bytes(long long cap, int buckets);
 SeamEdges seam_edges_carve(void *mem, long long cap, int buckets);
 // bound on the cross-tile edges of a tile grid (outward offsets per face)
 long long seam_edge_bound(const Geom &g, long long ntiles);
-void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, unsigned *err, int sm_count,
-                         cudaStream_t s);
+void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, long long merge_bound, unsigned *err,
+                         int sm_count, cudaStream_t s);
 
 struct BuildArgs {
     int dtype;

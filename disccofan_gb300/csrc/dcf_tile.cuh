@@ -216,7 +216,7 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
                         };
                         if (edge_implied(-dx, -dy, -dz, kp < kq ? kp : kq, key_at)) continue;
                     }
-                    connect_s(acc, p, qi, MERGE_BOUND_SMEM);
+                    connect_s(acc, p, qi, merge_bound_smem(g));
                 }
             }
             // levels are ordered for shorter merge walks, not for correctness:

@@ -147,8 +147,10 @@ dcf_status dcf_pattern_spectrum2d(dcf_ctx *ctx, dcf_tree *tree, int attr1, const
  * not wait on or fail in an allocation.  Its per-pixel scratch is a fixed 40 MiB
  * device array inside the library (held by every GPU that loads it until exit), so
  * the tree may have at most 8,388,608 pixels (DCF_ERR_INVALID beyond that).
- * out_device must be device memory.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.  All
+ * out_device must be device memory, and the tree must be on the context's device.
+ * The first call on a device looks up the array's device address (then cached
+ * for the life of the process: a caller that resets the device must not call it
+ * again); make that first call before any stream capture.  All
  * calls share the one array: calls that overlap on the GPU (other streams or
  * contexts) race and must not be issued concurrently. */
 dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, double lambda, int extract,

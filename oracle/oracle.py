@@ -30,11 +30,25 @@ PORT_SO = os.path.join(HERE, "_ref", "libdcforacle.so")
 RULES = {"direct": 0, "min": 1, "max": 2, "subtractive": 3}
 
 
+# The reference checkout the recipes compile from and CPU tests compare with:
+# $DCF_REFERENCE_DIR, else the build container's checkout location.  GPU machines have
+# no checkout; there reference_dir() is None and only the committed fixtures pin
+# the restatement.
+_DEFAULT_REFERENCE_DIR = "/root/reference"
+
+
+def reference_dir():
+    """Path of the reference checkout, or None when it is absent."""
+    d = os.environ.get("DCF_REFERENCE_DIR") or _DEFAULT_REFERENCE_DIR
+    return d if os.path.exists(os.path.join(d, "src", "sources", "flood.c")) else None
+
+
 def build(ref: bool = False) -> None:
     """Compile the oracle port (and, when asked and present, the reference)."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if ref and reference_dir():
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REFSRC=" + os.path.join(reference_dir(), "src")],
+                       check=True)
 
 
 def write_lvec(values, path=None) -> str:

@@ -174,7 +174,10 @@ def reference_case(ref: oracle.Reference, img: np.ndarray, conn: int, tree: str)
     return out
 
 
-def main(refdir: str = "/root/reference", outdir: str = HERE) -> None:
+def main(refdir: str | None = None, outdir: str = HERE) -> None:
+    refdir = refdir or oracle.reference_dir()
+    if refdir is None:
+        raise SystemExit("reference checkout not found (set DCF_REFERENCE_DIR)")
     ck = os.path.join(refdir, "tests", "checkimg")
     lena = np.flipud(read_png_gray8(os.path.join(ck, "input_image.png"))).copy()
     gt_area = np.flipud(read_png_gray8(os.path.join(ck, "GT_area_200.png"))).copy()

@@ -8,7 +8,9 @@ import pytest
 
 import disccofan_gb300 as dcf
 
-REF_CHECKIMG = "/root/reference/tests/checkimg"
+from oracle import oracle
+
+REF_CHECKIMG = os.path.join(oracle.reference_dir() or "", "tests", "checkimg")
 
 
 def write_fits(path, arr, bitpix, bzero=None, bscale=None):

@@ -179,6 +179,15 @@ def test_random_against_oracle(ctx, shape, kind, conn, tree):
     exact = kind in ("u8", "u16")
     for a in (1, 2, 3, 4, 5, 6, 7, 8, 12, 13, 14, 16, 17, 18):
         assert_attr(t.node_attribute(a), port.node_attr(a), a, exact, len(shape) == 3)
+    # 2-D spectrum on the bounding-box elongation (the headline's operation), and
+    # one on two extent attributes
+    for a1, v1, a2, v2 in ((18, [1.5, 2, 3, 5, 9], 0, [2, 4, 16, 64]), (3, [2, 3, 5, 9], 1, [3, 9, 27, 81])):
+        got = t.pattern_spectrum2d(a1, dcf.lvec_from_values(v1), a2, dcf.lvec_from_values(v2))
+        want = port.pattern2d(a1, v1, a2, v2)
+        if exact:
+            assert np.array_equal(got, want), (a1, a2)
+        else:
+            np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12 * np.abs(want).max(), err_msg=str((a1, a2)))
 
 
 def test_constant_image_single_node(ctx):

@@ -8,7 +8,7 @@ import pytest
 
 from oracle import oracle
 
-REF_SRC = "/root/reference/src/sources/flood.c"
+REF_DIR = oracle.reference_dir()
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
@@ -101,7 +101,7 @@ def test_eigen_restatement_diagonal_exact(port_lib):
 
 
 @pytest.mark.reference
-@pytest.mark.skipif(not os.path.exists(REF_SRC), reason="reference checkout not present")
+@pytest.mark.skipif(REF_DIR is None, reason="reference checkout not present")
 def test_port_matches_compiled_reference_random():
     oracle.build(ref=True)
     ref, port = oracle.Reference(), oracle.Port()
@@ -125,13 +125,13 @@ def test_port_matches_compiled_reference_random():
 def test_golden_fixtures_regenerate_identically(tmp_path):
     # the committed fixtures are exactly what tests/golden/make_golden.py makes from
     # the reference checkout and the reference compiled from it
-    if not os.path.exists(REF_SRC):
+    if REF_DIR is None:
         pytest.skip("reference checkout absent")
     import importlib.util
     spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
     mg = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mg)
-    mg.main(os.path.dirname(os.path.dirname(os.path.dirname(REF_SRC))), str(tmp_path))
+    mg.main(REF_DIR, str(tmp_path))
     for name in ("lena_fixtures.npz", "synthetic_reference.npz"):
         want, got = np.load(os.path.join(GOLDEN, name)), np.load(str(tmp_path / name))
         assert sorted(want.files) == sorted(got.files), name
