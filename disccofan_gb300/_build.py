@@ -31,6 +31,8 @@ def _deps() -> float:
     newest = 0.0
     for d in (CSRC, INCLUDE):
         for f in os.listdir(d):
+            if f in ("dcf_refshim.c", "dcf_reftypes.h"):  # the shim's own sources
+                continue
             newest = max(newest, os.path.getmtime(os.path.join(d, f)))
     return newest
 
@@ -53,19 +55,39 @@ def _compile(src: str, verbose: bool) -> str:
     return out
 
 
+SHIM_SRC = os.path.join(CSRC, "dcf_refshim.c")
+SHIM_LIB = os.path.join(HERE, "libdcf_refshim.so")
+
+
+def build_shim(verbose: bool = False) -> str:
+    """libdcf_refshim.so: the reference-signature replacement over libdcf_gb300.so
+    (include/dcf_reftypes.h layouts; the globals it reads come from the caller)."""
+    deps = [SHIM_SRC, os.path.join(INCLUDE, "dcf.h"), os.path.join(INCLUDE, "dcf_reftypes.h"), LIB]
+    if os.path.exists(SHIM_LIB) and os.path.getmtime(SHIM_LIB) >= max(os.path.getmtime(d) for d in deps):
+        return SHIM_LIB
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-Wall", "-Wextra", "-Werror", "-I" + INCLUDE, SHIM_SRC,
+           "-o", SHIM_LIB, "-L" + HERE, "-ldcf_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"shim build failed:\n{r.stdout}\n{r.stderr}")
+    return SHIM_LIB
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     units = CU_UNITS + C_UNITS
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), units))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc(), GENCODE, "-shared", "-o", LIB, *objs, "-lcudart"]
-    if verbose:
-        print(" ".join(cmd), flush=True)
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        cmd = [nvcc(), GENCODE, "-shared", "-o", LIB, *objs, "-lcudart"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_shim(verbose)
     return LIB
 
 

@@ -10,11 +10,11 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
+def declared_symbols(headers=("dcf.h",)):
     names = set()
     inc = os.path.join(ROOT, "include")
     for f in os.listdir(inc):
-        if f.endswith(".h"):
+        if f in headers:
             text = open(os.path.join(inc, f)).read()
             text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
             names |= set(re.findall(r"\b(dcf_[a-z0-9_]+)\s*\(", text))
