@@ -17,6 +17,8 @@
 // for 8/16-bit images and doubles otherwise.  Readouts (k_node_attr and the device
 // function attr_value) follow the reference's expressions operand by operand,
 // including which factors are float and which double.
+#include <cstdlib>
+
 #include "dcf_kernels.cuh"
 #include "dcf_attr_eval.cuh"
 
@@ -116,6 +118,118 @@ __global__ void k_attr_pixels(const float *__restrict__ gval, Geom g, const int 
                 atomicAdd((double *)a.gw[3] + node, gd * (double)y);
                 if (a.has_z) atomicAdd((double *)a.gw[4] + node, gd * (double)z);
             }
+        }
+    }
+}
+
+// Pixel pass of the area and extent groups on 2-D images, aggregated per tile.
+// A node's own pixels are its flat zone, which lies along its level contour: 32
+// pixels of a row belong to ~31 different nodes, so aggregating a warp's lanes
+// saves little.  Over a 64 x 64 tile the same node recurs (about 2 pixels per
+// node and tile on the 16384^2 u16 field), so each CTA first gathers its tile's
+// contributions by node in a shared-memory hash table (linear probing on the node
+// index; area count and bounding box per slot, shared-memory atomics), then issues
+// one set of global atomics per (tile, node).  Children are still counted into
+// `pending` with one global atomic per level root.  A slot search that finds the
+// table full (it holds as many slots as the tile has pixels, so it cannot be)
+// adds straight to the global records instead.
+constexpr int AGG_T = 64;                      // tile side
+constexpr int AGG_SLOTS = AGG_T * AGG_T;       // one slot per pixel of the tile
+constexpr int AGG_THREADS = 512;
+
+// DCF_TILE_AGG=0 in the environment selects the per-warp pixel pass instead (for
+// timing comparisons; both give the same records)
+static bool agg_enabled()
+{
+    static const bool on = [] {
+        const char *e = getenv("DCF_TILE_AGG");
+        return !e || atoi(e) != 0;
+    }();
+    return on;
+}
+
+template <int G>
+__host__ __device__ constexpr size_t agg_smem_bytes()
+{
+    return (size_t)AGG_SLOTS * 4 * (G == 1 ? 6 : 2);
+}
+
+template <int G>
+__global__ void __launch_bounds__(AGG_THREADS, G == 1 ? 2 : 4)
+k_attr_pixels_tiled(Geom g, const int *__restrict__ parent, const unsigned char *__restrict__ isroot, AttrBufs a,
+                    int ntx)
+{
+    extern __shared__ unsigned agg_smem[];
+    int *key = (int *)agg_smem;
+    unsigned *sarea = agg_smem + AGG_SLOTS;
+    unsigned *smnx = sarea + AGG_SLOTS, *smxx = smnx + AGG_SLOTS, *smny = smxx + AGG_SLOTS, *smxy = smny + AGG_SLOTS;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < AGG_SLOTS; i += AGG_THREADS) {
+        key[i] = NONE;
+        sarea[i] = 0u;
+        if (G == 1) {
+            smnx[i] = 0xFFFFFFFFu;
+            smny[i] = 0xFFFFFFFFu;
+            smxx[i] = 0u;
+            smxy[i] = 0u;
+        }
+    }
+    __syncthreads();
+    const int x0 = (blockIdx.x % ntx) * AGG_T, y0 = (blockIdx.x / ntx) * AGG_T;
+    // 16 warps: two per row of 64 pixels, eight rows per step
+    const int x = x0 + (warp & 1) * 32 + lane;
+    for (int r = warp >> 1; r < AGG_T; r += AGG_THREADS / 64) {
+        const int y = y0 + r;
+        const bool valid = x < g.W && y < g.H;  // warp-uniform rows; x may end mid-warp
+        const long long p = (long long)y * g.W + x;
+        const int par = valid ? parent[p] : NONE;
+        const bool root = valid && isroot[p];
+        const int node = valid ? (root ? (int)p : par) : -2;
+        if (root && par != NONE) atomicAdd(a.pending + par, 1);
+        const unsigned grp = __match_any_sync(0xffffffffu, node);
+        if (!valid || lane != __ffs(grp) - 1) continue;
+        const unsigned cnt = __popc(grp);
+        const unsigned mnx = (unsigned)x, mxx = (unsigned)(x - lane) + (unsigned)(32 - __clz(grp));
+        // slot of `node` (Fibonacci hashing of the index, linear probing)
+        unsigned h = ((unsigned)node * 2654435761u) >> 20;
+        int slot = NONE;
+        for (int probe = 0; probe < AGG_SLOTS; probe++) {
+            int k = ((volatile int *)key)[h];
+            if (k == NONE) k = atomicCAS(key + h, NONE, node);
+            if (k == NONE || k == node) {
+                slot = (int)h;
+                break;
+            }
+            h = (h + 1) & (AGG_SLOTS - 1);
+        }
+        if (slot == NONE) {  // unreachable with one slot per pixel; kept exact regardless
+            atomicAdd(a.area + node, cnt);
+            if (G == 1) {
+                atomicMin(a.bmin[0] + node, mnx);
+                atomicMax(a.bmax[0] + node, mxx);
+                atomicMin(a.bmin[1] + node, (unsigned)y);
+                atomicMax(a.bmax[1] + node, (unsigned)y + 1u);
+            }
+            continue;
+        }
+        atomicAdd(sarea + slot, cnt);
+        if (G == 1) {
+            atomicMin(smnx + slot, mnx);
+            atomicMax(smxx + slot, mxx);
+            atomicMin(smny + slot, (unsigned)y);
+            atomicMax(smxy + slot, (unsigned)y + 1u);
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < AGG_SLOTS; i += AGG_THREADS) {
+        const int node = key[i];
+        if (node == NONE) continue;
+        atomicAdd(a.area + node, sarea[i]);
+        if (G == 1) {
+            atomicMin(a.bmin[0] + node, smnx[i]);
+            atomicMax(a.bmax[0] + node, smxx[i]);
+            atomicMin(a.bmin[1] + node, smny[i]);
+            atomicMax(a.bmax[1] + node, smxy[i]);
         }
     }
 }
@@ -488,7 +602,25 @@ void launch_attributes(const TreeView &t, AttrBufs &a, unsigned *count, int up_s
     const int nb = grid_for(t.g.N, 256, sm);
 #define DCF_PIX(G, E) k_attr_pixels<G, E><<<nb, 256, 0, s>>>(t.gval, t.g, t.parent, t.isroot, a); note_launch()
     prof_begin(P_ATTR_PIX, s);
-    DCF_GROUP_SWITCH(DCF_PIX)
+    if (t.g.D == 1 && a.group <= 1 && agg_enabled()) {
+        const int ntx = (t.g.W + AGG_T - 1) / AGG_T, nty = (t.g.H + AGG_T - 1) / AGG_T;
+        if (a.group == 1) {
+            static bool attr_set = false;  // opt in to more than 48 KB of dynamic shared memory, once
+            if (!attr_set) {
+                cudaFuncSetAttribute(k_attr_pixels_tiled<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)agg_smem_bytes<1>());
+                attr_set = true;
+            }
+            k_attr_pixels_tiled<1><<<ntx * nty, AGG_THREADS, agg_smem_bytes<1>(), s>>>(t.g, t.parent, t.isroot, a,
+                                                                                      ntx);
+        } else {
+            k_attr_pixels_tiled<0><<<ntx * nty, AGG_THREADS, agg_smem_bytes<0>(), s>>>(t.g, t.parent, t.isroot, a,
+                                                                                      ntx);
+        }
+        note_launch();
+    } else {
+        DCF_GROUP_SWITCH(DCF_PIX)
+    }
 #undef DCF_PIX
     prof_end(P_ATTR_PIX, s);
     launch_attributes_up(t, a, count, up_steps, err, sm, s);

@@ -146,6 +146,7 @@ def test_shim_reproduces_reference_fixtures(tmp_path, lena):
     assert np.array_equal(load("check_ncomp.f32", np.float32).reshape(h, w), lena["check_ncomp_c4"])
     port = oracle.Port()
     port.load(img, 4, "max")
+    port.prepare(0)
     par = load("parent.i64", np.int64)
     assert np.array_equal(par, port.parent())
     # the tree file's level roots and their parents (GT_tree.txt)
