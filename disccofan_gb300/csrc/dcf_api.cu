@@ -132,6 +132,7 @@ struct dcf_tree {
     float *gval = nullptr;
     int *parent = nullptr;
     unsigned char *isroot = nullptr;
+    int *nodes = nullptr;                    // level roots in ascending order (node_list_bytes)
     unsigned *stats = nullptr;               // kmin, kmax, nans of the input
     unsigned long long *num_nodes = nullptr;
     AttrBufs attr;
@@ -389,6 +390,7 @@ dcf_status dcf_tree_destroy(dcf_tree *t)
     dev_free(t->gval, t->stream);
     dev_free(t->parent, t->stream);
     dev_free(t->isroot, t->stream);
+    dev_free(t->nodes, t->stream);
     dev_free(t->stats, t->stream);
     delete t;
     return DCF_OK;
@@ -403,6 +405,8 @@ static TreeView view_of(const dcf_tree *t)
     v.gval = t->gval;
     v.parent = t->parent;
     v.isroot = t->isroot;
+    v.nodes = t->nodes;
+    v.num_nodes = t->num_nodes;
     for (int i = 0; i < 3; i++) v.pixdim[i] = t->pixdim[i];
     v.integer_levels = t->dtype == U8 || t->dtype == U16;
     return v;
@@ -560,6 +564,7 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
     TRY(dmalloc_async(ctx, &t->gval, N * sizeof(float), ctx->stream));
     TRY(dmalloc_async(ctx, &t->parent, N * sizeof(int), ctx->stream));
     TRY(dmalloc_async(ctx, &t->isroot, N, ctx->stream));
+    TRY(dmalloc_async(ctx, &t->nodes, node_list_bytes((long long)N), ctx->stream));
     TRY(dmalloc_async(ctx, &t->stats, 4 * sizeof(unsigned) + sizeof(unsigned long long), ctx->stream));
     t->num_nodes = (unsigned long long *)(t->stats + 4);
     if (!img->on_device) {
@@ -586,6 +591,7 @@ dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_
         ba.node = (unsigned long long *)nodes;
         ba.parent = t->parent;
         ba.isroot = t->isroot;
+        ba.nodes = t->nodes;
         ba.num_nodes = t->num_nodes;
         ba.err = ctx->d_err;
         ba.sm_count = ctx->sm_count;
@@ -1131,6 +1137,7 @@ struct dcf_batch {
     unsigned long long *node = nullptr;
     int *parent = nullptr;
     unsigned char *isroot = nullptr;
+    int *nodes = nullptr;                    // level roots in ascending order (node_list_bytes)
     void *attr_mem = nullptr;
     AttrBufs attr;
     void *seam_mem = nullptr;                // level-ordered seam merge scratch
@@ -1195,6 +1202,8 @@ static TreeView batch_view(const dcf_batch *b)
     v.gval = b->gval;
     v.parent = b->parent;
     v.isroot = b->isroot;
+    v.nodes = b->nodes;
+    v.num_nodes = b->d_nodes;
     for (int i = 0; i < 3; i++) v.pixdim[i] = b->pixdim[i];
     v.integer_levels = b->dtype == U8 || b->dtype == U16;
     return v;
@@ -1280,7 +1289,7 @@ static dcf_status batch_forward(dcf_ctx *ctx, dcf_batch *b, const void *px, floa
     CU(cudaMemsetAsync(b->d_nodes, 0, sizeof(unsigned long long), s));
     launch_stats(b->dtype, px, b->N, b->d_misc + 2, b->d_misc + 3, b->d_misc + 4, sm, s);
     launch_batch_build(b->dtype, px, v.g, b->d_imgs, b->d_tiles, b->ntiles, b->chunk, b->d_misc, b->gval, b->node,
-                       b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, b->seam, sm, s);
+                       b->parent, b->isroot, b->d_nodes, b->nodes, ctx->d_err, b->ctas, b->seam, sm, s);
     CU(attr_zero(b->attr, (size_t)b->N, b->attr_mem, sm, s));
     launch_batch_attr_pixels(v.g, b->d_imgs, b->d_tiles, b->ntiles, b->gval, b->parent, b->isroot, b->attr, sm, s);
     unsigned *count = b->d_misc + 1;
@@ -1417,6 +1426,7 @@ dcf_status dcf_batch_create(dcf_ctx *ctx, int count, const uint32_t *widths, con
     BTRY(dmalloc(ctx, &b->node, (size_t)N * 8));
     BTRY(dmalloc(ctx, &b->parent, (size_t)N * 4));
     BTRY(dmalloc(ctx, &b->isroot, (size_t)N));
+    BTRY(dmalloc(ctx, &b->nodes, node_list_bytes(N)));
     BTRY(dmalloc(ctx, &b->attr_mem, attr_bytes(b->group, (size_t)N)));
     attr_carve(b->attr, b->group, dtype == U8 || dtype == U16, false, (size_t)N, b->attr_mem);
     BTRY(cudaMemcpy(b->d_imgs, b->imgs.data(), count * sizeof(BatchImg), cudaMemcpyHostToDevice));
@@ -1437,7 +1447,7 @@ dcf_status dcf_batch_destroy(dcf_batch *b)
     if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
     batch_drop_graph(b);
     void *bufs[] = {b->d_imgs, b->d_offs, b->d_tiles, b->d_misc, b->pixels, b->gval, b->node, b->parent, b->isroot,
-                    b->attr_mem, b->rest_mem, b->flag, b->target, b->filtered, b->spectra, b->lvec, b->adj_acc,
+                    b->nodes, b->attr_mem, b->rest_mem, b->flag, b->target, b->filtered, b->spectra, b->lvec, b->adj_acc,
                     b->adj_io, b->adj_w, b->seam_mem};
     for (void *p : bufs)
         if (p) cudaFree(p);
@@ -1517,7 +1527,7 @@ dcf_status dcf_batch_autotune(dcf_ctx *ctx, dcf_batch *b, const void *pixels, in
         for (int r = 0; r <= repeats; r++) {  // the first pass warms up
             cudaEventRecord(e0, ctx->stream);
             launch_batch_build(b->dtype, px, v.g, b->d_imgs, b->d_tiles, b->ntiles, b->chunk, b->d_misc, b->gval,
-                               b->node, b->parent, b->isroot, b->d_nodes, ctx->d_err, b->ctas, b->seam,
+                               b->node, b->parent, b->isroot, b->d_nodes, b->nodes, ctx->d_err, b->ctas, b->seam,
                                ctx->sm_count, ctx->stream);
             cudaEventRecord(e1, ctx->stream);
             dcf_status st = check_launch(ctx, 4);

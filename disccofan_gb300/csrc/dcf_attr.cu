@@ -247,12 +247,11 @@ void launch_fill_u32(long long n, uint32_t *dst, uint32_t v, int sm, cudaStream_
 }
 
 // leaves get pending = -1; nodes with exactly one child are flagged in `single`
-__global__ void k_mark_leaves(long long n, const unsigned char *__restrict__ isroot, int *pending,
+__global__ void k_mark_leaves(const int *__restrict__ nodes, const unsigned long long *num_nodes, int *pending,
                               unsigned char *single)
 {
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-         p += (long long)gridDim.x * blockDim.x) {
-        if (!isroot[p]) continue;
+    NODE_LOOP(p, nodes, num_nodes)
+    {
         const int c = pending[p];
         if (c == 0) pending[p] = -1;
         single[p] = c == 1;
@@ -356,12 +355,13 @@ constexpr int STALLED = -3;         // pending value of a complete node not fold
 // nodes still waiting for children) lies near the root and is finished by pointer
 // jumping (k_jump_fold).
 template <int G, bool EXACT>
-__global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs a, int up_steps, unsigned *err)
+__global__ void k_attr_up(const int *__restrict__ nodes, const unsigned long long *num_nodes,
+                          const int *__restrict__ parent, AttrBufs a, int up_steps, unsigned *err)
 {
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-         p += (long long)gridDim.x * blockDim.x) {
+    NODE_LOOP(p, nodes, num_nodes)
+    {
         if (__ldcg(a.pending + p) != -1) continue;
-        int u = (int)p;
+        int u = p;
         Rec<G, EXACT> r;
         rec_load<G, EXACT>(a, u, r);
         for (int step = 0;; step++) {
@@ -390,12 +390,11 @@ __global__ void k_attr_up(long long n, const int *__restrict__ parent, AttrBufs 
 
 // nodes left for the pointer-jumping phase, listed in any order
 // (list entries beyond cap are dropped and flagged: the caller sized the list)
-__global__ void k_collect_rest(long long n, const unsigned char *__restrict__ isroot, int *pending, int *list,
-                               unsigned *count, unsigned cap, unsigned *err)
+__global__ void k_collect_rest(const int *__restrict__ nodes, const unsigned long long *num_nodes, int *pending,
+                               int *list, unsigned *count, unsigned cap, unsigned *err)
 {
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-         p += (long long)gridDim.x * blockDim.x) {
-        if (!isroot[p]) continue;
+    NODE_LOOP(p, nodes, num_nodes)
+    {
         int s = pending[p];
         if (s > 0 || s == STALLED) {
             unsigned i = atomicAdd(count, 1u);
@@ -587,12 +586,12 @@ void launch_attributes_up(const TreeView &t, AttrBufs &a, unsigned *count, int u
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_ATTR_UP, s);
-    k_mark_leaves<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, a.single); note_launch();
-#define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.g.N, t.parent, a, up_steps, err); note_launch()
+    k_mark_leaves<<<nb, 256, 0, s>>>(t.nodes, t.num_nodes, a.pending, a.single); note_launch();
+#define DCF_UP(G, E) k_attr_up<G, E><<<nb, 256, 0, s>>>(t.nodes, t.num_nodes, t.parent, a, up_steps, err); note_launch()
     DCF_GROUP_SWITCH(DCF_UP)
 #undef DCF_UP
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, nullptr, count, 0u, err); note_launch();
+    k_collect_rest<<<nb, 256, 0, s>>>(t.nodes, t.num_nodes, a.pending, nullptr, count, 0u, err); note_launch();
     prof_end(P_ATTR_UP, s);
 }
 
@@ -648,7 +647,7 @@ static void rest_phase(const TreeView &t, AttrBufs &a, unsigned cap, bool, unsig
     cudaMemsetAsync(act, 0, 33 * sizeof(unsigned), s);
     cudaMemsetAsync(act, 1, 1, s);
     cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-    k_collect_rest<<<nb, 256, 0, s>>>(t.g.N, t.isroot, a.pending, list, count, cap, err); note_launch();
+    k_collect_rest<<<nb, 256, 0, s>>>(t.nodes, t.num_nodes, a.pending, list, count, cap, err); note_launch();
     if (cap == 0) return;
     const int rb = grid_for(cap, 256, sm);
     k_rest_gather<G><<<rb, 256, 0, s>>>(list, count, cap, t.parent, a.pending, a, r0, j0, err); note_launch();

@@ -279,8 +279,8 @@ __global__ void k_batch_spectrum(Geom bg, const BatchImg *__restrict__ imgs, con
 
 void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchImg *imgs, const BatchTile *tiles,
                         int ntiles, int chunk, unsigned *next, float *gval, unsigned long long *node, int *parent,
-                        unsigned char *isroot, unsigned long long *num_nodes, unsigned *err, int ctas_per_sm,
-                        SeamEdges &seam, int sm, cudaStream_t s)
+                        unsigned char *isroot, unsigned long long *num_nodes, int *nodes, unsigned *err,
+                        int ctas_per_sm, SeamEdges &seam, int sm, cudaStream_t s)
 {
     const int grid = sm * ctas_per_sm;
     cudaMemsetAsync(next, 0, sizeof(unsigned), s);
@@ -308,7 +308,7 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
         k_batch_seam<<<grid_for(work, 128, sm), 128, 0, s>>>(node, bg, imgs, tiles, ntiles, err); note_launch();
     }
     prof_end(P_SEAM, s);
-    launch_canon(node, bg, parent, isroot, num_nodes, err, sm, s);
+    launch_canon(node, bg, parent, isroot, num_nodes, nodes, err, sm, s);
 }
 
 void launch_batch_attr_pixels(const Geom &bg, const BatchImg *imgs, const BatchTile *tiles, int ntiles,

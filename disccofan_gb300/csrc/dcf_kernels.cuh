@@ -47,6 +47,20 @@ template <typename T> struct TileCfg {
     static constexpr int word_bytes = narrow ? 4 : 8;
 };
 
+// the level roots of a tree (TreeView::nodes, TreeView::num_nodes)
+struct NodeSet {
+    const int *nodes;
+    const unsigned long long *num;
+};
+
+// Grid-stride loop over the level roots that launch_canon listed (nodes[0 ..
+// *num_nodes), ascending): `u` is the node's pixel index.  `continue` in the body
+// moves to the next node.
+#define NODE_LOOP(u, nodes, num_nodes)                                                                         \
+    for (long long _nl_i = blockIdx.x * (long long)blockDim.x + threadIdx.x, _nl_m = (long long)*(num_nodes); \
+         _nl_i < _nl_m; _nl_i += (long long)gridDim.x * blockDim.x)                                           \
+        for (int u = (nodes)[_nl_i], _nl_once = 1; _nl_once; _nl_once = 0)
+
 inline int grid_for(long long n, int block, int sm_count)
 {
     long long b = (n + block - 1) / block;
@@ -95,12 +109,16 @@ struct BuildArgs {
     int *parent;
     unsigned char *isroot;
     unsigned long long *num_nodes;
+    int *nodes;                      // level-root list (node_list_bytes(N) bytes)
     unsigned *err;
     int sm_count;
     SeamEdges seam;                  // level-ordered seam merge scratch (buckets == 0: direct merge)
 };
+// canonical form, then the level roots listed in ascending index order into
+// `nodes` (a buffer of node_list_bytes(N) bytes: the list, then chunk counts)
+size_t node_list_bytes(long long n);
 void launch_canon(unsigned long long *node, const Geom &g, int *parent, unsigned char *isroot,
-                  unsigned long long *num_nodes, unsigned *err, int sm_count, cudaStream_t s);
+                  unsigned long long *num_nodes, int *nodes, unsigned *err, int sm_count, cudaStream_t s);
 
 void launch_stats(int dtype, const void *img, long long n, unsigned *kmin, unsigned *kmax, unsigned *nans,
                   int sm_count, cudaStream_t s);
@@ -122,8 +140,8 @@ struct BatchTile {
 // tiles per queue grab), seam merge inside each cutout, canonical form
 void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchImg *imgs, const BatchTile *tiles,
                         int ntiles, int chunk, unsigned *next, float *gval, unsigned long long *node, int *parent,
-                        unsigned char *isroot, unsigned long long *num_nodes, unsigned *err, int ctas_per_sm,
-                        SeamEdges &seam, int sm_count, cudaStream_t s);
+                        unsigned char *isroot, unsigned long long *num_nodes, int *nodes, unsigned *err,
+                        int ctas_per_sm, SeamEdges &seam, int sm_count, cudaStream_t s);
 // bound on a batch's cross-tile edges (capacity of its SeamEdges)
 long long batch_seam_edge_bound(const Geom &bg, const BatchImg *imgs_host, int count);
 
@@ -163,6 +181,8 @@ struct TreeView {
     const float *gval;
     const int *parent;
     const unsigned char *isroot;
+    const int *nodes;                // the level roots, ascending (launch_canon)
+    const unsigned long long *num_nodes;  // device: their count
     float pixdim[3];
     bool integer_levels;             // u8/u16 input: level arithmetic is exact in float
 };

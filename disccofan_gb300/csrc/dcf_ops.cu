@@ -26,24 +26,23 @@ constexpr int UNKNOWN = -2;
 #define GRID_LOOP(p, n) \
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < (n); p += (long long)gridDim.x * blockDim.x)
 
-__global__ void k_flag(Geom g, const unsigned char *__restrict__ isroot, AttrBufs a, int attr, double lambda,
+__global__ void k_flag(Geom g, NodeSet ns, AttrBufs a, int attr, double lambda,
                        float pd0, float pd1, float pd2, unsigned char *flag, int *target)
 {
     const float pd[3] = {pd0, pd1, pd2};
-    GRID_LOOP(p, g.N)
+    NODE_LOOP(p, ns.nodes, ns.num)
     {
         target[p] = UNKNOWN;
-        if (!isroot[p]) continue;
         flag[p] = attr_value(a, attr, (int)p, pd) >= lambda ? 1 : 0;
     }
 }
 
-__global__ void k_mark_kept(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+__global__ void k_mark_kept(Geom g, NodeSet ns, const int *__restrict__ parent,
                             const unsigned char *__restrict__ flag, unsigned *kept, unsigned *err)
 {
-    GRID_LOOP(p, g.N)
+    NODE_LOOP(p, ns.nodes, ns.num)
     {
-        if (!isroot[p] || !flag[p]) continue;
+        if (!flag[p]) continue;
         int u = (int)p;
         long long it = 0;
         for (; it < g.N && u != NONE; it++) {
@@ -56,12 +55,11 @@ __global__ void k_mark_kept(Geom g, const unsigned char *__restrict__ isroot, co
 
 // nearest flagged ancestor-or-self; flag may be a byte array or the kept words
 template <typename F>
-__global__ void k_resolve(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+__global__ void k_resolve(Geom g, NodeSet ns, const int *__restrict__ parent,
                           const F *__restrict__ flag, int *target, unsigned *err)
 {
-    GRID_LOOP(p, g.N)
+    NODE_LOOP(p, ns.nodes, ns.num)
     {
-        if (!isroot[p]) continue;
         if (((volatile int *)target)[p] != UNKNOWN) continue;
         int v = (int)p, res = NONE;
         long long it = 0;
@@ -81,13 +79,12 @@ __global__ void k_resolve(Geom g, const unsigned char *__restrict__ isroot, cons
 
 // subtractive: value(u) = sum over the root path of delta(w), delta(w) =
 // flag ? gval(w) - gval(parent(w)) : 0, the root's delta being flag ? gval : 0.
-__global__ void k_sub_init(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+__global__ void k_sub_init(Geom g, NodeSet ns, const int *__restrict__ parent,
                            const float *__restrict__ gval, const unsigned char *__restrict__ flag, int *jump,
                            double *acc)
 {
-    GRID_LOOP(p, g.N)
+    NODE_LOOP(p, ns.nodes, ns.num)
     {
-        if (!isroot[p]) continue;
         int q = parent[p];
         jump[p] = q;
         double d = 0.0;
@@ -96,12 +93,11 @@ __global__ void k_sub_init(Geom g, const unsigned char *__restrict__ isroot, con
     }
 }
 
-__global__ void k_jump_sum(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ jin,
+__global__ void k_jump_sum(Geom g, NodeSet ns, const int *__restrict__ jin,
                            const double *__restrict__ ain, int *jout, double *aout)
 {
-    GRID_LOOP(p, g.N)
+    NODE_LOOP(p, ns.nodes, ns.num)
     {
-        if (!isroot[p]) continue;
         int j = jin[p];
         if (j == NONE) {
             jout[p] = NONE;
@@ -167,24 +163,22 @@ __global__ void k_sub_exact(Geom g, const unsigned char *__restrict__ isroot, co
 }
 
 // min rule: best(u) = topmost removed node on u's path, root excluded
-__global__ void k_min_init(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+__global__ void k_min_init(Geom g, NodeSet ns, const int *__restrict__ parent,
                            const unsigned char *__restrict__ flag, int *jump, int *best)
 {
-    GRID_LOOP(p, g.N)
+    NODE_LOOP(p, ns.nodes, ns.num)
     {
-        if (!isroot[p]) continue;
         int q = parent[p];
         jump[p] = q;
         best[p] = (q != NONE && !flag[p]) ? (int)p : NONE;
     }
 }
 
-__global__ void k_jump_last(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ jin,
+__global__ void k_jump_last(Geom g, NodeSet ns, const int *__restrict__ jin,
                             const int *__restrict__ bin, int *jout, int *bout)
 {
-    GRID_LOOP(p, g.N)
+    NODE_LOOP(p, ns.nodes, ns.num)
     {
-        if (!isroot[p]) continue;
         int j = jin[p];
         if (j == NONE) {
             jout[p] = NONE;
@@ -239,17 +233,17 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
-    k_flag<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
+    k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
                               w.target); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
     const double *accp = nullptr;
     if (rule == 0) {
-        k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err); note_launch();
+        k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
     } else if (rule == 2) {
         cudaMemsetAsync(w.kept, 0, t.g.N * sizeof(unsigned), s);
-        k_mark_kept<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.kept, err); note_launch();
-        k_resolve<unsigned><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.kept, w.target, err); note_launch();
+        k_mark_kept<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.kept, err); note_launch();
+        k_resolve<unsigned><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.kept, w.target, err); note_launch();
     } else {
         const int R = rounds_for(depth_bound);
         int *j0 = w.jump, *j1 = w.jump2;
@@ -270,18 +264,18 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
             rule = 4;
         } else if (rule == 3) {
             double *a0 = w.acc, *a1 = w.acc2;
-            k_sub_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, j0, a0); note_launch();
+            k_sub_init<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, t.gval, w.flag, j0, a0); note_launch();
             for (int r = 0; r < R; r++) {
-                k_jump_sum<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, a0, j1, a1); note_launch();
+                k_jump_sum<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, j0, a0, j1, a1); note_launch();
                 int *tj = j0; j0 = j1; j1 = tj;
                 double *ta = a0; a0 = a1; a1 = ta;
             }
             accp = a0;
         } else {
             int *b0 = w.target, *b1 = w.best2;
-            k_min_init<<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, j0, b0); note_launch();
+            k_min_init<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, j0, b0); note_launch();
             for (int r = 0; r < R; r++) {
-                k_jump_last<<<nb, 256, 0, s>>>(t.g, t.isroot, j0, b0, j1, b1); note_launch();
+                k_jump_last<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, j0, b0, j1, b1); note_launch();
                 int *tj = j0; j0 = j1; j1 = tj;
                 int *tb = b0; b0 = b1; b1 = tb;
             }
@@ -345,7 +339,7 @@ constexpr int SPEC_SMEM_BINS = 4096;
 // one __reduce_add_sync each) and their leader issues one shared-memory 64-bit
 // integer atomic; otherwise every node adds its double term on its own.
 template <bool EXACT>
-__global__ void k_spectrum(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
+__global__ void k_spectrum(Geom g, NodeSet ns, const int *__restrict__ parent,
                            const float *__restrict__ gval, AttrBufs a, int a1, const float *__restrict__ l1, int n1,
                            int a2, const float *__restrict__ l2, int n2, float pd0, float pd1, float pd2,
                            double *spec)
@@ -361,13 +355,14 @@ __global__ void k_spectrum(Geom g, const unsigned char *__restrict__ isroot, con
     if (EXACT) {
         const int lane = threadIdx.x & 31;
         const long long wstride = (long long)gridDim.x * blockDim.x;
+        const long long m = (long long)*ns.num;
         // whole warps iterate together so the match below sees the full warp
-        for (long long base = (blockIdx.x * (long long)blockDim.x + threadIdx.x) - lane; base < g.N;
+        for (long long base = (blockIdx.x * (long long)blockDim.x + threadIdx.x) - lane; base < m;
              base += wstride) {
-            const long long p = base + lane;
+            const int p = base + lane < m ? ns.nodes[base + lane] : NONE;
             int bin = -1;
             unsigned long long v = 0;
-            if (p < g.N && isroot[p]) {
+            if (p != NONE) {
                 const int q = parent[p];
                 const float dh = q != NONE ? __fsub_rn(gval[p], gval[q]) : gval[p];
                 if (dh != 0.0f) {
@@ -389,9 +384,8 @@ __global__ void k_spectrum(Geom g, const unsigned char *__restrict__ isroot, con
             else atomicAdd(spec + bin, (double)sum);
         }
     } else {
-        GRID_LOOP(p, g.N)
+        NODE_LOOP(p, ns.nodes, ns.num)
         {
-            if (!isroot[p]) continue;
             const int q = parent[p];
             const float dh = q != NONE ? __fsub_rn(gval[p], gval[q]) : gval[p];
             if (dh == 0.0f) continue;
@@ -421,10 +415,10 @@ void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *
     const bool exact = t.integer_levels && t.pixdim[0] == 1.0f && t.pixdim[1] == 1.0f && t.pixdim[2] == 1.0f;
     prof_begin(P_SPECTRUM, s);
     if (exact)
-        k_spectrum<true><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
+        k_spectrum<true><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
                                             t.pixdim[1], t.pixdim[2], spec);
     else
-        k_spectrum<false><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
+        k_spectrum<false><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
                                              t.pixdim[1], t.pixdim[2], spec);
     note_launch();
     prof_end(P_SPECTRUM, s);
@@ -652,11 +646,11 @@ void launch_direct_targets(const TreeView &t, const AttrBufs &a, int attr, doubl
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
-    k_flag<<<nb, 256, 0, s>>>(t.g, t.isroot, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
+    k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
                               w.target); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(P_RESOLVE, s);
-    k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, w.flag, w.target, err); note_launch();
+    k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
     prof_end(P_RESOLVE, s);
 }
 
