@@ -106,6 +106,8 @@ def library() -> C.CDLL:
         "dcf_tree_gval": [vp, vp, vp, i],
         "dcf_node_attribute": [vp, vp, i, i, vp, i],
         "dcf_filter": [vp, vp, i, i, d, i, vp, i],
+        "dcf_filter_as": [vp, vp, i, i, d, i, i, vp, i],
+        "dcf_image_stage": [vp, C.POINTER(_Image), C.POINTER(_Image)],
         "dcf_attribute_check": [vp, vp, i, vp, i],
         "dcf_dmp": [vp, vp, i, i, vp, i, vp, i],
         "dcf_pattern_spectrum": [vp, vp, i, vp, i, vp, i],
@@ -260,8 +262,34 @@ class Context:
 
     def build(self, image, connectivity: int = 4, tree_type: str = "max", attribute: int = 0,
               pixdim=(1.0, 1.0, 1.0)) -> "Tree":
-        """build_tree_with_attributes: tree of a 2-D (H, W) or 3-D (D, H, W) image."""
+        """build_tree_with_attributes: tree of a 2-D (H, W) or 3-D (D, H, W) image
+        (numpy array, CUDA tensor, or a StagedImage from stage())."""
         return Tree(self, image, connectivity, tree_type, attribute, pixdim)
+
+    def stage(self, image) -> "StagedImage":
+        """dcf_image_stage: copy a host image to this context's device buffer once,
+        for several builds (valid until the next stage() on this context)."""
+        arr = np.ascontiguousarray(image)
+        if arr.dtype not in DTYPES:
+            raise TypeError(f"unsupported image dtype {arr.dtype} (u8, u16, u32, f32)")
+        if arr.ndim not in (2, 3):
+            raise ValueError("image must be 2-D or 3-D")
+        d, h, w = (1,) + arr.shape if arr.ndim == 2 else arr.shape
+        im = _Image(arr.ctypes.data, DTYPES[arr.dtype], 0, (C.c_uint64 * 3)(w, h, d), 4, 0,
+                    (C.c_float * 3)(1.0, 1.0, 1.0))
+        out = _Image()
+        self.check(self.lib.dcf_image_stage(self.h, C.byref(im), C.byref(out)), "dcf_image_stage")
+        return StagedImage(out, arr.shape, arr.dtype, arr)
+
+
+class StagedImage:
+    """An image copied to a context's device buffer by Context.stage()."""
+
+    def __init__(self, im, shape, dtype, host):
+        self.im = im
+        self.shape = tuple(shape)
+        self.dtype = np.dtype(dtype)
+        self._host = host  # the copy is stream-ordered: keep the source alive
 
     def batch(self, shapes, dtype=np.float32, connectivity: int = 8, attribute: int = 0,
               pixdim=(1.0, 1.0, 1.0)) -> "Batch":
@@ -274,7 +302,13 @@ class Tree:
         self.ctx = ctx
         L = ctx.lib
         on_dev = _is_torch_cuda(image)
-        if on_dev:
+        if isinstance(image, StagedImage):
+            on_dev = True
+            dt = image.dtype
+            ptr = image.im.data
+            shape = image.shape
+            self._keep = image
+        elif on_dev:
             import torch
             tdt = {torch.uint8: np.uint8, torch.uint16: np.uint16, torch.int32: None,
                    torch.float32: np.float32}.get(image.dtype)
@@ -386,12 +420,29 @@ class Tree:
         return a
 
     # -- operations (operation.c) ------------------------------------------
-    def filter(self, attribute: int, lam: float, rule="direct", extract: bool = False, out=None):
+    def filter(self, attribute: int, lam: float, rule="direct", extract: bool = False, out=None, out_dtype=None):
+        """tree_filtering (+ extract, min-tree re-inversion).  The output is float32,
+        or, with out_dtype (or an `out` array) of the input's own uint8/uint16 type,
+        that type (dcf_filter_as)."""
         self._ensure_group(attribute)
         r = RULES[rule] if isinstance(rule, str) else int(rule)
-        a, p, dev = self._out(np.float32, out)
-        self.ctx.check(self.ctx.lib.dcf_filter(self.ctx.h, self.h, attribute, r, float(lam), int(extract), p, dev),
-                       "filter")
+        if out is not None and out_dtype is None:
+            odt = getattr(out, "dtype", None)
+            if odt is not None and "uint16" in str(odt):
+                out_dtype = np.uint16
+            elif odt is not None and "uint8" in str(odt):
+                out_dtype = np.uint8
+        if out_dtype is None or np.dtype(out_dtype) == np.float32:
+            a, p, dev = self._out(np.float32, out)
+            self.ctx.check(self.ctx.lib.dcf_filter(self.ctx.h, self.h, attribute, r, float(lam), int(extract), p,
+                                                   dev), "filter")
+            return self._shape(a)
+        odt = np.dtype(out_dtype)
+        if odt not in DTYPES:
+            raise TypeError(f"unsupported output dtype {odt}")
+        a, p, dev = self._out(odt, out)
+        self.ctx.check(self.ctx.lib.dcf_filter_as(self.ctx.h, self.h, attribute, r, float(lam), int(extract),
+                                                  DTYPES[odt], p, dev), "filter_as")
         return self._shape(a)
 
     def check(self, attribute: int, out=None):

@@ -58,6 +58,7 @@ struct dcf_ctx {
     std::mutex trees_mu;
     std::set<dcf_tree *> trees;       // live trees; orphaned (stream cleared) when the context goes
     DevBuf scratch[16];               // reusable work buffers (filter, spectra, attributes, seams)
+    DevBuf stage;                     // the image staged by dcf_image_stage (stream-ordered pool memory)
     bool prof_on = false;
     ProfEvent *prof_ev = nullptr;     // recorded events, in launch order
     int prof_n = 0, prof_cap = 0;
@@ -318,6 +319,7 @@ dcf_status dcf_ctx_destroy(dcf_ctx *ctx)
         for (dcf_tree *t : ctx->trees) orphan_tree(t);
         ctx->trees.clear();
     }
+    if (ctx->stage.p) cudaFreeAsync(ctx->stage.p, ctx->stream);
     for (auto &b : ctx->scratch)
         if (b.p) cudaFree(b.p);
     for (int i = 0; i < ctx->prof_cap; i++) cudaEventDestroy(ctx->prof_ev[i].ev);
@@ -864,7 +866,7 @@ static long long depth_bound(const dcf_tree *t)
 }
 
 static dcf_status run_filter(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, double lambda, int extract,
-                             float *dst)
+                             void *dst, int out_dtype = F32)
 {
     const size_t N = (size_t)t->g.N;
     FilterWork w{};
@@ -897,8 +899,59 @@ static dcf_status run_filter(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, 
     }
     TreeView v = view_of(t);
     launch_filter(v, t->attr, attr_idx, rule, lambda, extract != 0, dst, w, depth_bound(t), ctx->d_err,
-                  ctx->sm_count, ctx->stream);
+                  ctx->sm_count, ctx->stream, out_dtype);
     return check_launch(ctx, 3);
+}
+
+dcf_status dcf_filter_as(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, double lambda, int extract,
+                         int out_dtype, void *out, int on_device)
+{
+    ActiveScope active_scope_(ctx);
+    if (!ctx || !t || !out) return DCF_ERR_INVALID;
+    if (rule < 0 || rule > 3) return set_err(ctx, DCF_ERR_INVALID, "bad rule %d", rule);
+    if (out_dtype != DCF_F32 && !((out_dtype == DCF_U8 || out_dtype == DCF_U16) && out_dtype == t->dtype))
+        return set_err(ctx, DCF_ERR_INVALID, "output type %d: float, or the input's own u8/u16 type", out_dtype);
+    dcf_status st = check_attr(ctx, t, attr_idx);
+    if (st != DCF_OK) return st;
+    static const size_t esize[4] = {1, 2, 4, 4};
+    const size_t bytes = (size_t)t->g.N * esize[out_dtype];
+    void *dst = out;
+    if (!on_device && (st = scratch(ctx, 7, bytes, &dst)) != DCF_OK) return st;
+    if ((st = run_filter(ctx, t, attr_idx, rule, lambda, extract, dst, out_dtype)) != DCF_OK) return st;
+    if (!on_device) {
+        CU(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if ((st = sync_and_check(ctx)) != DCF_OK) return st;
+        return check_nan(ctx, t, nullptr);
+    }
+    return DCF_OK;
+}
+
+dcf_status dcf_image_stage(dcf_ctx *ctx, const dcf_image *in, dcf_image *out)
+{
+    if (!ctx || !in || !out || !in->data) return DCF_ERR_INVALID;
+    if (in->dtype < DCF_U8 || in->dtype > DCF_F32) return set_err(ctx, DCF_ERR_INVALID, "bad dtype %d", in->dtype);
+    *out = *in;
+    if (in->on_device) return DCF_OK;
+    const uint64_t D = in->dims[2] ? in->dims[2] : 1;
+    if (in->dims[0] > 0x7FFFFFFF || in->dims[1] > 0x7FFFFFFF || D > 0x7FFFFFFF ||
+        in->dims[0] * in->dims[1] >= 0x7FFFFFFFull || in->dims[0] * in->dims[1] * D >= 0x7FFFFFFFull)
+        return set_err(ctx, DCF_ERR_INVALID, "image too large");
+    static const size_t esize[4] = {1, 2, 4, 4};
+    const size_t bytes = (size_t)(in->dims[0] * in->dims[1] * D) * esize[in->dtype];
+    CU(cudaSetDevice(ctx->device));
+    DevBuf &b = ctx->stage;
+    if (b.bytes < bytes) {
+        // earlier builds may still read the old buffer: free it in stream order
+        if (b.p) CU(cudaFreeAsync(b.p, ctx->stream));
+        b.p = nullptr;
+        b.bytes = 0;
+        CU(dmalloc_async(ctx, &b.p, bytes, ctx->stream));
+        b.bytes = bytes;
+    }
+    CU(cudaMemcpyAsync(b.p, in->data, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    out->data = b.p;
+    out->on_device = 1;
+    return DCF_OK;
 }
 
 dcf_status dcf_filter(dcf_ctx *ctx, dcf_tree *t, int attr_idx, int rule, double lambda, int extract, float *out,

@@ -233,9 +233,10 @@ struct FilterWork {
     unsigned *remaining = nullptr;  // exact subtractive rule: nodes still unresolved
 };
 
+// out: N pixels of out_dtype (F32; U8 or U16 only for trees of u8 / u16 images)
 void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, double lambda, bool extract,
-                   float *out, const FilterWork &w, long long depth_bound, unsigned *err, int sm_count,
-                   cudaStream_t s);
+                   void *out, const FilterWork &w, long long depth_bound, unsigned *err, int sm_count,
+                   cudaStream_t s, int out_dtype = F32);
 void launch_check(const TreeView &t, const AttrBufs &a, int attr, float *out, int sm_count, cudaStream_t s);
 void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *l1, int n1, int a2,
                      const float *l2, int n2, double *spec, int sm_count, cudaStream_t s);

@@ -191,11 +191,18 @@ __global__ void k_jump_last(Geom g, NodeSet ns, const int *__restrict__ jin,
     }
 }
 
-template <int RULE>
+// output pixel in the caller's type: float, or (for u8/u16 trees, whose every
+// filtered level is an integer in the input's range) the input's own integer type
+template <typename O> __device__ __forceinline__ O out_value(float v);
+template <> __device__ __forceinline__ float out_value<float>(float v) { return v; }
+template <> __device__ __forceinline__ uint16_t out_value<uint16_t>(float v) { return (uint16_t)min(__float2uint_rn(v), 65535u); }
+template <> __device__ __forceinline__ uint8_t out_value<uint8_t>(float v) { return (uint8_t)min(__float2uint_rn(v), 255u); }
+
+template <int RULE, typename O>
 __global__ void k_filter_out(Geom g, const unsigned char *__restrict__ isroot, const int *__restrict__ parent,
                              const float *__restrict__ gval, const unsigned char *__restrict__ flag,
                              const int *__restrict__ target, const double *__restrict__ acc, bool extract,
-                             bool tree_min, const unsigned *kmax, float *out)
+                             bool tree_min, const unsigned *kmax, O *out)
 {
     const float gmax = tree_min ? key_to_level(*kmax) : 0.0f;
     GRID_LOOP(p, g.N)
@@ -217,7 +224,7 @@ __global__ void k_filter_out(Geom g, const unsigned char *__restrict__ isroot, c
         }
         if (extract) val = __fsub_rn(gval[p], val);
         if (tree_min) val = __fsub_rn(gmax, val);
-        out[p] = val;
+        out[p] = out_value<O>(val);
     }
 }
 
@@ -229,7 +236,8 @@ static int rounds_for(long long depth_bound)
 }
 
 void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, double lambda, bool extract,
-                   float *out, const FilterWork &w, long long depth_bound, unsigned *err, int sm, cudaStream_t s)
+                   void *out, const FilterWork &w, long long depth_bound, unsigned *err, int sm, cudaStream_t s,
+                   int out_dtype)
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
@@ -284,8 +292,18 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     }
     prof_end(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
     prof_begin(P_FILTER_OUT, s);
-#define DCF_OUT(R) \
-    k_filter_out<R><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, w.target, accp, extract, t.tree_min, t.kmax, out); note_launch()
+#define DCF_OUT_T(R, O)                                                                                      \
+    {                                                                                                        \
+        k_filter_out<R, O><<<nb, 256, 0, s>>>(t.g, t.isroot, t.parent, t.gval, w.flag, w.target, accp, extract, \
+                                              t.tree_min, t.kmax, (O *)out);                                 \
+        note_launch();                                                                                       \
+    }
+#define DCF_OUT(R)                                            \
+    do {                                                      \
+        if (out_dtype == U16) DCF_OUT_T(R, uint16_t)          \
+        else if (out_dtype == U8) DCF_OUT_T(R, uint8_t)       \
+        else DCF_OUT_T(R, float)                              \
+    } while (0)
     switch (rule) {
     case 0: DCF_OUT(0); break;
     case 1: DCF_OUT(1); break;
@@ -294,6 +312,7 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     default: DCF_OUT(4); break;
     }
 #undef DCF_OUT
+#undef DCF_OUT_T
     prof_end(P_FILTER_OUT, s);
 }
 

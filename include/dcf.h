@@ -102,6 +102,14 @@ const char *dcf_profile_kernel_name(int id);
 /* Build the max-tree (min-tree: of the inverted image) with the attribute group
  * of attr_idx.  The image is copied to the device when on_device == 0. */
 dcf_status dcf_tree_build(dcf_ctx *ctx, const dcf_image *img, int attr_idx, dcf_tree **out);
+/* Copy a host image to the context's device staging buffer once, for several
+ * builds from the same pixels (the max- and the min-tree of one image): *out is
+ * *in with data pointing at the staged copy and on_device = 1.  The copy is
+ * ordered on the context's stream; the staged image stays valid until the next
+ * dcf_image_stage on this context or its destruction.  An image already on the
+ * device is returned unchanged.  (No reference counterpart: the reference reads
+ * its input once into Node.gval.) */
+dcf_status dcf_image_stage(dcf_ctx *ctx, const dcf_image *in, dcf_image *out);
 /* Accumulate the attribute group of attr_idx on the existing tree (no rebuild). */
 dcf_status dcf_tree_set_attribute(dcf_ctx *ctx, dcf_tree *tree, int attr_idx);
 dcf_status dcf_tree_destroy(dcf_tree *tree);
@@ -123,6 +131,13 @@ dcf_status dcf_node_attribute(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, int ar
  * min-tree re-inversion g_max - out.  out: width*height*depth floats. */
 dcf_status dcf_filter(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, int rule, double lambda, int extract,
                       float *out, int on_device);
+/* dcf_filter with the output in out_dtype: DCF_F32, or, for a tree of a DCF_U8 /
+ * DCF_U16 image, that same type -- every filtered value of such an image is an
+ * integer of its range, and the reference writes 8/16-bit outputs in the input's
+ * depth (write_basic, io.c:1802-1841) -- which halves or quarters the bytes read
+ * back.  Other types: DCF_ERR_INVALID. */
+dcf_status dcf_filter_as(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, int rule, double lambda, int extract,
+                         int out_dtype, void *out, int on_device);
 /* out[p] = (float) attribute of p's node. */
 dcf_status dcf_attribute_check(dcf_ctx *ctx, dcf_tree *tree, int attr_idx, float *out, int on_device);
 /* Differential morphological profile: for each lvec[i+1], i < num_lambdas-1,

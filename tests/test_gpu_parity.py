@@ -190,6 +190,34 @@ def test_random_against_oracle(ctx, shape, kind, conn, tree):
             np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12 * np.abs(want).max(), err_msg=str((a1, a2)))
 
 
+@pytest.mark.parametrize("kind,conn,tree", [("u8", 4, "max"), ("u16", 8, "min"), ("u16", 8, "max")])
+def test_filter_in_input_type_and_staged_builds(ctx, kind, conn, tree):
+    # dcf_filter_as: every rule (and extract) in the input's own integer type equals
+    # the float output exactly; dcf_image_stage: trees built from one staged copy
+    # equal trees built from the host image
+    rng = np.random.default_rng(21)
+    img = rand_image(rng, (150, 170), kind)
+    staged = ctx.stage(img)
+    t = gpu_tree(ctx, img, conn, tree, attr=18)
+    for tt in (tree, "max" if tree == "min" else "min"):
+        ts = gpu_tree(ctx, staged, conn, tt, attr=18)
+        th = gpu_tree(ctx, img, conn, tt, attr=18)
+        assert np.array_equal(ts.parent(), th.parent()), tt
+        assert np.array_equal(ts.filter(0, 30.0), th.filter(0, 30.0)), tt
+    for rule in range(4):
+        for extract in (False, True):
+            f = t.filter(0, 30.0, rule, extract=extract)
+            g = t.filter(0, 30.0, rule, extract=extract, out_dtype=img.dtype)
+            assert g.dtype == img.dtype
+            assert np.array_equal(g.astype(np.float32), f), (rule, extract)
+    with pytest.raises(dcf.DcfError) as e:
+        t.filter(0, 30.0, out_dtype=np.uint32)
+    assert e.value.status == 1
+    if kind == "u16":
+        with pytest.raises(dcf.DcfError):
+            t.filter(0, 30.0, out_dtype=np.uint8)
+
+
 def test_constant_image_single_node(ctx):
     img = np.full((37, 91), 7, np.uint8)
     t = gpu_tree(ctx, img, 8)
