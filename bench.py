@@ -19,8 +19,8 @@ host memory and the filtered images + spectra read back every step.  Inputs are
 
 `--impl reference` times the reference's CPU path: the oracle restatement of the
 reference's flooding, seam merge, filter and spectrum (oracle/dcf_oracle.c, pinned
-bit-exact against the reference's own code), on all host threads, on a crop of the
-same image.
+bit-exact against the reference's own code), on all host threads, on the whole
+16384^2 image (--ref-reps full-size steps), plus a one-thread figure on a crop.
 """
 from __future__ import annotations
 
@@ -61,6 +61,16 @@ def max_over_ranks(values, device):
     t = torch.tensor(values, dtype=torch.float64, device=device)
     torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     return [float(x) for x in t]
+
+
+def load_dram_profile():
+    """Per-kernel DRAM bytes per launch measured by ncu on the 4096^2 crop of the
+    main workload (profiles/dram_c2_4096_u16.json), or None."""
+    p = os.path.join(ROOT, "profiles", "dram_c2_4096_u16.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
 
 
 def load_peaks():
@@ -235,16 +245,21 @@ def run_ours(args):
     ctx.set_profiling(False)
     ctx.synchronize()
 
-    # e2e through the public API: pinned host image in, filtered images + spectra out
+    # e2e through the public API: the pinned host image is staged on the device once
+    # per step (dcf_image_stage) for both trees; the filtered images come back in
+    # the input's own uint16 type (dcf_filter_as, as the reference writes a 16-bit
+    # input's output) and the spectra as doubles
     h_img = torch.empty((size, size), dtype=img.dtype, pin_memory=True)
     h_img.copy_(img)
     h_img_np = h_img.numpy() if img.dtype != torch.int32 else h_img.numpy().astype(np.uint16)
-    h_out = [torch.empty(npix, dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+    h_out = [torch.empty(npix, dtype=torch.uint16 if hasattr(torch, "uint16") else torch.int16,
+                         pin_memory=True).numpy().view(np.uint16) for _ in range(2)]
     h_spec = [np.zeros((l_area.size, l_elong.size), np.float64) for _ in range(2)]
 
     def e2e_step():
+        staged = ctx.stage(h_img_np)
         for k, tt in enumerate(("max", "min")):
-            t = ctx.build(h_img_np, connectivity=8, tree_type=tt, attribute=18)
+            t = ctx.build(staged, connectivity=8, tree_type=tt, attribute=18)
             t.filter(0, 1000.0, "direct", out=h_out[k])
             h_spec[k][:] = 0
             t.pattern_spectrum2d(18, l_elong, 0, l_area, out=h_spec[k])
@@ -258,41 +273,50 @@ def run_ours(args):
         e2e_step()
     barrier()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / max(e2e_steps, 1)
-    h2d = 2 * npix * img.element_size()
-    d2h = 2 * (npix * 4 + h_spec[0].nbytes)
+    h2d = npix * img.element_size()
+    d2h = 2 * (h_out[0].nbytes + h_spec[0].nbytes)
 
     if world > 1:
         ms, e2e_ms = max_over_ranks([ms, e2e_ms], "cuda")
     if rank != 0:
         return None
 
-    # roofline of the dominant kernel: algorithmic bytes per launch / event-timed duration
+    # Roofline.  Algorithmic bytes are the compulsory I/O of one tree: the u16 image
+    # in, a 4-byte parent and the u16 filtered image out, and a 12-byte record
+    # (area + 2-D bounding box) per node: B_tree = N (2 + 4 + 2) + 12 M, plus 8 bytes
+    # per spectrum bin.  The dominant kernel's `achieved` is B_tree / its mean
+    # duration per launch (one launch per tree, the max and min trees alternating,
+    # so M is their mean); `kernel_bytes` is that kernel's own minimum traffic.
     peak, peak_kind = load_peaks()
     s_in = 2
     dom, (dom_ms, dom_n) = max(prof.items(), key=lambda kv: kv[1][0])
     total_prof = sum(v[0] for v in prof.values())
     M = sum(node_counts) / 2.0
-    per_launch = {
-        "tile_build": npix * (s_in + 4 + 8),        # image in; level and node word out
-        "seam_merge": npix * (4 + 4) * 0.047,       # shell pixels: parent + level read (2-D, 64x64 tiles)
-        "canonicalise": npix * (4 + 4 + 1),         # parent read+write, root flag
-        "attr_pixels": npix * (4 + 1) + M * 12,     # parent + root flag in, area+bbox records out
-        "attr_bottom_up": M * (12 + 4 + 4),         # records folded once, parent + counter per node
-        "attr_pointer_jump": M * (12 + 4),
-        "filter_flag": M * 12 + npix * 1,
+    nbins = l_area.size * l_elong.size
+    B_tree = npix * (s_in + 4 + s_in) + 12 * M + 8 * nbins
+    B_alg = 2 * B_tree
+    kernel_bytes = {
+        "tile_build": npix * (s_in + 4 + 8),        # image in; level and 64-bit node word out
+        "seam_merge": None,                          # chain walks: no fixed byte count
+        "canonicalise": npix * (8 + 4 + 1),         # node words in, parent and root flag out
+        "attr_pixels": npix * (4 + 1) + M * 12,     # parent + root flag in, area + bbox records out
+        "attr_bottom_up": M * (12 + 4 + 4),
         "filter_resolve": M * (4 + 4),
-        "filter_out": npix * (4 + 4 + 4),           # parent + target in, float image out
-        "spectrum": M * (12 + 4 + 4) + 8 * 441,
-        "stats": npix * s_in,
-    }
-    alg = per_launch.get(dom, npix * s_in)
-    # DRAM bytes per pixel per launch from one ncu capture of the kernel on a
-    # 4096^2 uint16 image (profiles/k_tile_build_4096_u16.md), scaled by pixels:
-    # traffic grows with the pixel count for this per-pixel pass
-    dram_per_px = {"tile_build": (33.69472e6 + 154.18496e6) / 4096 ** 2}
-    traffic = round(dram_per_px[dom] * npix) if dom in dram_per_px else None
-    achieved = alg / (dom_ms / dom_n * 1e-3) / 1e9
-    B_alg = 2 * (npix * (s_in + 4 + s_in) + 12 * M) + 2 * 8 * 441
+        "filter_out": npix * (4 + 4 + 2),
+        "spectrum": M * (12 + 4 + 4) + 8 * nbins,
+    }.get(dom)
+    achieved = B_tree / (dom_ms / dom_n * 1e-3) / 1e9
+    dram = load_dram_profile()
+    traffic = None
+    pipeline_traffic = None
+    if dram:
+        # DRAM bytes per pixel per launch of each kernel, from ncu on the 4096^2
+        # crop of this workload, scaled by pixels (per-pixel passes; node passes
+        # scale with the node count, which is proportional to the pixels here)
+        scale = npix / dram["pixels"]
+        if dom in dram["per_launch_bytes"]:
+            traffic = round(dram["per_launch_bytes"][dom] * scale)
+        pipeline_traffic = round(sum(dram["per_launch_bytes"].values()) * scale * 2)
     result = {
         "metric": METRIC,
         "value": round(world * npix / 1e6 / (ms * 1e-3), 3),
@@ -313,13 +337,20 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "pipeline_roofline": {"alg_bytes_per_step": B_alg,
                                          "achieved_gbs": round(B_alg / (ms * 1e-3) / 1e9, 2),
-                                         "frac": round(B_alg / (ms * 1e-3) / 1e9 / peak, 5)},
+                                         "frac": round(B_alg / (ms * 1e-3) / 1e9 / peak, 5),
+                                         "dram_bytes_per_step": pipeline_traffic,
+                                         "traffic_ratio": None if pipeline_traffic is None else
+                                         round(pipeline_traffic / B_alg, 3),
+                                         "dram_source": dram["source"] if dram else None},
                    "kernel_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sorted(prof.items())}},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": traffic,
-                     "traffic_source": "ncu DRAM read+write of one 4096^2 launch, scaled by pixels",
+                     "traffic_source": None if traffic is None else
+                     "ncu DRAM read+write of one 4096^2 launch, scaled by pixels",
                      "share": round(dom_ms / total_prof, 4) if total_prof else None,
-                     "alg_bytes_per_launch": alg, "peak_source": f"{peak_kind} hbm_gbs"},
+                     "alg_bytes_per_launch": round(B_tree), "kernel_bytes": kernel_bytes,
+                     "alg_bytes_basis": "per tree: N*(2 in + 4 parent + 2 filtered) + 12*M + 8*bins",
+                     "peak_source": f"{peak_kind} hbm_gbs"},
         "e2e": None if args.no_e2e else {
             "value": round(world * npix / 1e6 / (e2e_ms * 1e-3), 3), "unit": "Mpx/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
@@ -327,7 +358,7 @@ def run_ours(args):
         "clocks": clk.summary(),
     }
     if not args.no_cpu:
-        result["cpu_baseline"] = cpu_baseline(img, args.cpu_sample, reps=1)
+        result["cpu_baseline"] = cpu_baseline(img, args.cpu_sample, reps=1, ctx=ctx)
     del img, d_out, d_spec, h_img
     log(f"main workload: {ms:.1f} ms/step")
     if not args.no_batch:
@@ -630,28 +661,53 @@ def run_adjoint(args, ctx, stream):
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle restatement of the reference's path, all host threads
 # ---------------------------------------------------------------------------
-def cpu_baseline(img_dev, sample: int, reps: int = 1, threads: int | None = None):
+def oracle_step(img_f32, threads: int, npix_bins: int):
+    """The main workload's step on the host: the oracle restatement of the reference's
+    build, area filter and 2-D spectrum (bins of the full image), max and min tree.
+    Returns (seconds, {tree: (filtered, spectrum)})."""
+    from oracle import oracle
+    l_el = list(np.geomspace(1, 16384, 20))
+    l_ar = list(np.geomspace(1, npix_bins, 20))
+    out = {}
+    t0 = time.perf_counter()
+    for tt in ("max", "min"):
+        p = oracle.Port(threads=threads)
+        p.load(img_f32, 8, tt, threads=threads)
+        out[tt] = (p.filter(0, 1000.0, 0), p.pattern2d(18, l_el, 0, l_ar))
+        del p
+    return time.perf_counter() - t0, out
+
+
+def cpu_baseline(img_dev, sample: int, reps: int = 1, threads: int | None = None, ctx=None):
+    """The oracle on a sample x sample crop of the image on all host threads; with a
+    context, the GPU path runs on the same crop and `parity_vs_gpu` says whether the
+    filtered images and spectra of both trees are identical."""
     from oracle import oracle
     oracle.build(ref=False)
+    npix_full = img_dev.shape[0] * img_dev.shape[1]
     crop = img_dev[:sample, :sample].to("cpu").numpy().astype(np.float32) if hasattr(img_dev, "to") else \
         np.asarray(img_dev[:sample, :sample], np.float32)
     threads = threads or os.cpu_count() or 1
-    l_el = list(np.geomspace(1, 16384, 20))
-    l_ar = list(np.geomspace(1, crop.size, 20))
-    times = []
+    times, outs = [], None
     for _ in range(reps):
-        t0 = time.perf_counter()
-        for tt in ("max", "min"):
-            p = oracle.Port(threads=threads)
-            p.load(crop, 8, tt, threads=threads)
-            p.filter(0, 1000.0, 0)
-            p.pattern2d(18, l_el, 0, l_ar)
-            del p
-        times.append(time.perf_counter() - t0)
+        secs, outs = oracle_step(crop, threads, npix_full)
+        times.append(secs)
     best = min(times)
-    return {"value": round(crop.size / 1e6 / best, 3), "unit": "Mpx/s", "cores": threads, "kind": "port",
-            "sample": f"{sample}x{sample} crop of the same image, max+min tree, same ops; best of {reps}",
-            "seconds_per_step": round(best, 3)}
+    res = {"value": round(crop.size / 1e6 / best, 3), "unit": "Mpx/s", "cores": threads, "kind": "port",
+           "sample": f"{sample}x{sample} crop of the same image, max+min tree, same ops; best of {reps}",
+           "seconds_per_step": round(best, 3)}
+    if ctx is not None and hasattr(img_dev, "to"):
+        l_elong, l_area = lvecs(npix_full)
+        dev = img_dev[:sample, :sample].contiguous()
+        same = True
+        for tt in ("max", "min"):
+            t = ctx.build(dev, connectivity=8, tree_type=tt, attribute=18)
+            f = t.filter(0, 1000.0, "direct")
+            s = t.pattern_spectrum2d(18, l_elong, 0, l_area)
+            t.close()
+            same = same and np.array_equal(f, outs[tt][0]) and np.array_equal(s, outs[tt][1])
+        res["parity_vs_gpu"] = bool(same)
+    return res
 
 
 def run_reference(args):
@@ -659,24 +715,40 @@ def run_reference(args):
     if rank != 0:
         return None
     import torch
-    if torch.cuda.is_available():
-        img = make_image(args.size, seed=2, device="cuda")[:args.cpu_sample, :args.cpu_sample].to("cpu")
-    else:
-        img = make_image(args.cpu_sample, seed=2, device="cpu")
-    img = img.numpy().astype(np.float32)
-    for _ in range(args.warmup):
-        cpu_baseline(img, args.cpu_sample)
-    vals = []
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(img, args.cpu_sample))
-    secs = statistics.median(v["seconds_per_step"] for v in vals)
+    from oracle import oracle
+    oracle.build(ref=False)
+    size = args.size
+    # the same image as our arm (generated on the GPU when there is one: the FFT
+    # and the sources are identical to ours), then held in host memory as the
+    # reference holds every pixel, float32
+    img = make_image(size, seed=2, device="cuda" if torch.cuda.is_available() else "cpu")
+    img = img.to("cpu").numpy().astype(np.float32)
+    threads = os.cpu_count() or 1
+    # Each full-size step (both trees, ~80 s on 16 cores) is timed as a whole; the
+    # --steps/--warmup counts would make this arm take half an hour, so
+    # --ref-reps full-size steps are timed (default 1) with no warm-up: the
+    # oracle's only warm-up effect is first-touch of its host buffers, which
+    # each step pays again anyway (its trees are freed after every step)
+    reps = max(1, args.ref_reps)
+    times = [oracle_step(img, threads, img.size)[0] for _ in range(reps)]
+    secs = statistics.median(times)
     v = round(img.size / 1e6 / secs, 3)
-    cb = dict(vals[0])
-    cb["value"] = v
+    # one host thread, on a 1024^2 crop (bins of the full image)
+    s1 = min(1024, size)
+    crop = np.ascontiguousarray(img[:s1, :s1])
+    secs1 = oracle_step(crop, 1, img.size)[0]
+    sample = (f"the whole {size}x{size} image, max+min tree, same ops, {threads} host threads; "
+              f"{reps} full-size step(s) timed (median), not --steps")
+    cb = {"value": v, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample,
+          "seconds_per_step": round(secs, 3),
+          "single_thread": {"value": round(crop.size / 1e6 / secs1, 3), "unit": "Mpx/s", "cores": 1,
+                            "sample": f"{s1}x{s1} crop, max+min tree, same ops", "seconds": round(secs1, 3)}}
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mpx/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
-            "data": "synthetic (same generator, crop)", "config": {"workload": WORKLOAD, "sample": cb["sample"]},
+            "data": "synthetic: the same seeded image as the GPU arm",
+            "config": {"workload": WORKLOAD if size == 16384 else WORKLOAD.replace("16384", str(size)),
+                       "sample": sample},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -688,6 +760,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--ref-reps", type=int, default=1, help="--impl reference: full-size steps timed")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-cutout workload")

@@ -47,7 +47,7 @@ def test_max_over_ranks_gloo_world2():
 def test_reference_arm_prints_once_under_torchrun(port_lib):
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(free_port()), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-sample", "256"]
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--size", "512"]
     env = dict(os.environ, CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS="2")
     r = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
