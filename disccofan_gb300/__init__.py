@@ -282,6 +282,12 @@ class Context:
         return StagedImage(out, arr.shape, arr.dtype, arr)
 
 
+    def batch(self, shapes, dtype=np.float32, connectivity: int = 8, attribute: int = 0,
+              pixdim=(1.0, 1.0, 1.0)) -> "Batch":
+        """A batch of 2-D cutouts; shapes = [(height, width), ...]."""
+        return Batch(self, shapes, dtype, connectivity, attribute, pixdim)
+
+
 class StagedImage:
     """An image copied to a context's device buffer by Context.stage()."""
 
@@ -290,11 +296,6 @@ class StagedImage:
         self.shape = tuple(shape)
         self.dtype = np.dtype(dtype)
         self._host = host  # the copy is stream-ordered: keep the source alive
-
-    def batch(self, shapes, dtype=np.float32, connectivity: int = 8, attribute: int = 0,
-              pixdim=(1.0, 1.0, 1.0)) -> "Batch":
-        """A batch of 2-D cutouts; shapes = [(height, width), ...]."""
-        return Batch(self, shapes, dtype, connectivity, attribute, pixdim)
 
 
 class Tree:
