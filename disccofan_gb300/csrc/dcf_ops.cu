@@ -16,6 +16,8 @@
 //   k_spectrum      per level root: dh = gval - gval(parent) in float, bins by
 //                   binary search (pattern.c:7-24), dh * area accumulated in a
 //                   shared-memory histogram per block, flushed with global atomics.
+#include <cstdlib>
+
 #include "dcf_kernels.cuh"
 #include "dcf_attr_eval.cuh"
 
@@ -351,6 +353,127 @@ __device__ __forceinline__ int find_scale(const float *lv, int n, double v)
 
 constexpr int SPEC_SMEM_BINS = 4096;
 
+// ---------------------------------------------------------------------------
+// Exact bin search without double arithmetic (GB300 runs FP64 at a small fraction
+// of its FP32 rate, and the double readouts and comparisons made the spectrum
+// FP64-pipe bound).  With integer levels and unit pixel sizes the binned values
+// are exact numbers that can be compared with each float threshold lambda_i
+// exactly, so the predicate v >= (double)lambda_i of find_scale -- and therefore
+// the bisection's result -- is unchanged:
+//   BK_INT    an integer below 2^53 (a group's area readout in groups 1-4, the
+//             rectangle area, the x/y/z extents): v >= lambda <=> v >= ceil(lambda);
+//   BK_FLOAT  area_attribute with unit pixels is (float) area: compared in float;
+//   BK_RATIO  bounding-box elongation hi / max(lo, 1), hi >= lo integers: with
+//             lambda = M 2^-S (M its 24-bit mantissa) hi / lo' >= lambda <=>
+//             hi 2^S >= M lo' in 64-bit integers.  The double quotient the
+//             reference compares falls on the same side of the float threshold:
+//             a quotient below lambda is below it by at least 2^-S / lo', more than
+//             half an ulp of lambda while lo' <= 2^30 (lo' <= min(W, H) < 2^16 for any
+//             image under 2^31 pixels);
+//   BK_GENERIC any other attribute: the double readout and comparison.
+// ---------------------------------------------------------------------------
+enum BinKind : int { BK_GENERIC = 0, BK_INT = 1, BK_FLOAT = 2, BK_RATIO = 3 };
+constexpr int SPEC_FAST_MAXBINS = 128;        // thresholds kept in shared memory per vector
+constexpr unsigned long long TH_NEVER = ~0ull;
+
+// value kind of binning attribute `attr` (< 0: the group's area readout) of a tree
+// of u8/u16 levels with unit pixels
+static int bin_kind(int group, int attr)
+{
+    if (attr < 0) return group == 0 ? BK_FLOAT : BK_INT;
+    if (attr == 0) return BK_FLOAT;
+    if (group == 1 && (attr == 1 || attr == 3 || attr == 4 || attr == 5)) return BK_INT;
+    if (group == 1 && attr == 18) return BK_RATIO;
+    return BK_GENERIC;
+}
+
+// integer value v >= lambda <=> v >= th (TH_NEVER: never)
+__device__ __forceinline__ unsigned long long int_threshold(float lam)
+{
+    if (lam != lam) return TH_NEVER;
+    if (!(lam > 0.0f)) return 0ull;
+    const float c = ceilf(lam);
+    if (c >= 18446744073709551616.0f) return TH_NEVER;
+    return __float2ull_rz(c);
+}
+
+// ratio threshold: kind 0 compares hi << s >= m * lo'; 1 always true; 2 never
+struct RatioTh {
+    unsigned long long m;
+    int s;
+    int kind;
+};
+__device__ __forceinline__ RatioTh ratio_threshold(float lam)
+{
+    RatioTh r{0ull, 0, 2};
+    if (lam != lam) return r;                  // NaN: nothing compares >= it
+    if (lam <= 1.0f) {                         // every elongation is >= 1
+        r.kind = 1;
+        return r;
+    }
+    if (lam >= 2147483648.0f) return r;        // above any hi / lo' (hi < 2^31)
+    const unsigned bits = __float_as_uint(lam);
+    const int e = (int)((bits >> 23) & 0xFF) - 127;  // lam in [2^e, 2^(e+1)), 0 <= e <= 30
+    const unsigned long long mant = (bits & 0x7FFFFFu) | 0x800000u;
+    r.kind = 0;
+    if (e <= 23) {
+        r.m = mant;
+        r.s = 23 - e;
+    } else {  // lam is the integer mant * 2^(e-23)
+        r.m = mant << (e - 23);
+        r.s = 0;
+    }
+    return r;
+}
+
+__device__ __forceinline__ bool ratio_ge(unsigned hi, unsigned lo1, const RatioTh &t)
+{
+    if (t.kind != 0) return t.kind == 1;
+    return ((unsigned long long)hi << t.s) >= t.m * (unsigned long long)lo1;
+}
+
+// the bisection of find_scale (pattern.c:7-24) over a predicate ge(i) = "value >= lambda_i"
+template <class GE>
+__device__ __forceinline__ int find_scale_pred(int n, GE ge)
+{
+    int upper = n - 1, lower = 0;
+    if (ge(upper)) return upper;
+    int mid = (upper + lower) / 2;
+    while (mid != lower) {
+        if (ge(mid)) lower = mid;
+        else upper = mid;
+        mid = (upper + lower) / 2;
+    }
+    return lower;
+}
+
+struct BinTh {
+    unsigned long long it[SPEC_FAST_MAXBINS];
+    RatioTh rt[SPEC_FAST_MAXBINS];
+};
+
+// bin of node u on lambda vector lv (n values) for a value of kind `kind` != BK_GENERIC
+__device__ __forceinline__ int fast_bin(const AttrBufs &a, int attr, int kind, int u, const float *lv, int n,
+                                        const BinTh &th)
+{
+    if (kind == BK_INT) {
+        unsigned long long v;
+        if (attr < 0) v = a.area[u];
+        else if (attr == 1)
+            v = (unsigned long long)(a.bmax[0][u] - a.bmin[0][u]) * (a.bmax[1][u] - a.bmin[1][u]) *
+                (a.bmax[2][u] - a.bmin[2][u]);
+        else v = a.bmax[attr - 3][u] - a.bmin[attr - 3][u];
+        return find_scale_pred(n, [&](int i) { return th.it[i] != TH_NEVER && v >= th.it[i]; });
+    }
+    if (kind == BK_FLOAT) {
+        const float f = __uint2float_rn(a.area[u]);
+        return find_scale_pred(n, [&](int i) { return f >= lv[i]; });
+    }
+    const unsigned xe = a.bmax[0][u] - a.bmin[0][u], ye = a.bmax[1][u] - a.bmin[1][u];
+    const unsigned hi = xe > ye ? xe : ye, lo = xe < ye ? xe : ye, lo1 = lo > 1u ? lo : 1u;
+    return find_scale_pred(n, [&](int i) { return ratio_ge(hi, lo1, th.rt[i]); });
+}
+
 // EXACT: u8/u16 levels and unit pixel sizes, so every dh * area is an integer below
 // 2^48 and every bin's sum is below 2^53 (the sum of all bins is the image's grey
 // sum): any summation order gives the reference's double sums bit for bit.  The
@@ -358,10 +481,10 @@ constexpr int SPEC_SMEM_BINS = 4096;
 // one __reduce_add_sync each) and their leader issues one shared-memory 64-bit
 // integer atomic; otherwise every node adds its double term on its own.
 template <bool EXACT>
-__global__ void k_spectrum(Geom g, NodeSet ns, const int *__restrict__ parent,
+__global__ void __launch_bounds__(256, 3) k_spectrum(Geom g, NodeSet ns, const int *__restrict__ parent,
                            const float *__restrict__ gval, AttrBufs a, int a1, const float *__restrict__ l1, int n1,
                            int a2, const float *__restrict__ l2, int n2, float pd0, float pd1, float pd2,
-                           double *spec)
+                           double *spec, int k1, int k2)
 {
     __shared__ double hist[SPEC_SMEM_BINS];
     unsigned long long *ihist = (unsigned long long *)hist;
@@ -372,6 +495,19 @@ __global__ void k_spectrum(Geom g, NodeSet ns, const int *__restrict__ parent,
     __syncthreads();
     const float pd[3] = {pd0, pd1, pd2};
     if (EXACT) {
+        // thresholds of both lambda vectors for the exact-arithmetic bin search (BinKind)
+        __shared__ BinTh th[2];
+        for (int i = threadIdx.x; i < SPEC_FAST_MAXBINS; i += blockDim.x) {
+            if (k1 != BK_GENERIC && i < n1) {
+                th[0].it[i] = int_threshold(l1[i]);
+                th[0].rt[i] = ratio_threshold(l1[i]);
+            }
+            if (k2 != BK_GENERIC && i < n2) {
+                th[1].it[i] = int_threshold(l2[i]);
+                th[1].rt[i] = ratio_threshold(l2[i]);
+            }
+        }
+        __syncthreads();
         const int lane = threadIdx.x & 31;
         const long long wstride = (long long)gridDim.x * blockDim.x;
         const long long m = (long long)*ns.num;
@@ -385,11 +521,18 @@ __global__ void k_spectrum(Geom g, NodeSet ns, const int *__restrict__ parent,
                 const int q = parent[p];
                 const float dh = q != NONE ? __fsub_rn(gval[p], gval[q]) : gval[p];
                 if (dh != 0.0f) {
-                    const double ar = area_value(a, (int)p, pd);
-                    const int s1 = find_scale(l1, n1, a1 < 0 ? ar : attr_value(a, a1, (int)p, pd));
-                    const int s2 = n2 <= 1 ? 0 : find_scale(l2, n2, a2 < 0 ? ar : attr_value(a, a2, (int)p, pd));
+                    const int s1 = k1 != BK_GENERIC ? fast_bin(a, a1, k1, p, l1, n1, th[0])
+                                                    : find_scale(l1, n1, a1 < 0 ? area_value(a, p, pd)
+                                                                                : attr_value(a, a1, p, pd));
+                    const int s2 = n2 <= 1             ? 0
+                                   : k2 != BK_GENERIC ? fast_bin(a, a2, k2, p, l2, n2, th[1])
+                                                      : find_scale(l2, n2, a2 < 0 ? area_value(a, p, pd)
+                                                                                  : attr_value(a, a2, p, pd));
                     bin = s1 + s2 * n1;
-                    v = (unsigned long long)((double)dh * ar);
+                    // dh times the group's area readout, both integers (group 0 reads
+                    // the area through float, an integer too)
+                    const unsigned ar = a.group == 0 ? __float2uint_rn(__uint2float_rn(a.area[p])) : a.area[p];
+                    v = (unsigned long long)__float2uint_rn(dh) * ar;
                 }
             }
             const unsigned grp = __match_any_sync(0xffffffffu, bin);
@@ -432,13 +575,21 @@ void launch_spectrum(const TreeView &t, const AttrBufs &a, int a1, const float *
 {
     const int nb = grid_for(t.g.N, 256, sm);
     const bool exact = t.integer_levels && t.pixdim[0] == 1.0f && t.pixdim[1] == 1.0f && t.pixdim[2] == 1.0f;
+    // the exact-arithmetic bin search, per lambda vector (BinKind); DCF_SPEC_FP64=1 in
+    // the environment keeps the double search (for timing comparisons)
+    static const bool fp64 = [] {
+        const char *e = getenv("DCF_SPEC_FP64");
+        return e && atoi(e) != 0;
+    }();
+    const int k1 = exact && !fp64 && n1 <= SPEC_FAST_MAXBINS ? bin_kind(a.group, a1) : BK_GENERIC;
+    const int k2 = exact && !fp64 && n2 <= SPEC_FAST_MAXBINS ? bin_kind(a.group, a2) : BK_GENERIC;
     prof_begin(P_SPECTRUM, s);
     if (exact)
-        k_spectrum<true><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
-                                            t.pixdim[1], t.pixdim[2], spec);
+        k_spectrum<true><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, t.gval, a, a1, l1, n1, a2,
+                                            l2, n2, t.pixdim[0], t.pixdim[1], t.pixdim[2], spec, k1, k2);
     else
-        k_spectrum<false><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, t.gval, a, a1, l1, n1, a2, l2, n2, t.pixdim[0],
-                                             t.pixdim[1], t.pixdim[2], spec);
+        k_spectrum<false><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, t.gval, a, a1, l1, n1, a2,
+                                             l2, n2, t.pixdim[0], t.pixdim[1], t.pixdim[2], spec, k1, k2);
     note_launch();
     prof_end(P_SPECTRUM, s);
 }
