@@ -438,13 +438,18 @@ static void attr_carve(AttrBufs &a, int group, bool exact_g, bool has_z, size_t 
         for (int d = 0; d < 6; d++) a.s2[d] = (unsigned long long *)take64();
     }
     if (group == 3 || group == 4) for (int d = 0; d < 5; d++) a.gw[d] = take64();
-    auto take32 = [&]() { void *p = m; m += 4 * N; return p; };
-    a.area = (uint32_t *)take32();
-    a.pending = (int *)take32();
-    if (group == 1) {
-        for (int d = 0; d < 3; d++) a.bmin[d] = (uint32_t *)take32();
-        for (int d = 0; d < 3; d++) a.bmax[d] = (uint32_t *)take32();
-    }
+    // the 32-bit fields interleaved per node (Field): the extent group's record is
+    // area, pending, bmin x/y/z, bmax x/y/z; the other groups pair area and pending
+    const int words = group == 1 ? REC1_WORDS : 2;
+    uint32_t *rec = (uint32_t *)m;
+    m += 4 * (size_t)words * N;
+    a.area = Field<uint32_t>{rec, words};
+    a.pending = Field<int>{(int *)rec + 1, words};
+    if (group == 1)
+        for (int d = 0; d < 3; d++) {
+            a.bmin[d] = Field<uint32_t>{rec + 2 + d, words};
+            a.bmax[d] = Field<uint32_t>{rec + 5 + d, words};
+        }
     a.single = (unsigned char *)m;
 }
 
@@ -452,10 +457,7 @@ static void attr_carve(AttrBufs &a, int group, bool exact_g, bool has_z, size_t 
 static cudaError_t attr_zero(const AttrBufs &a, size_t N, void *mem, int sm, cudaStream_t s)
 {
     cudaError_t e = cudaMemsetAsync(mem, 0, attr_bytes(a.group, N) - 256, s);
-    if (e == cudaSuccess && a.group == 1) {
-        e = cudaMemsetAsync(a.bmin[0], 0xFF, (a.has_z ? 3 : 2) * 4 * N, s);
-        if (!a.has_z) launch_fill_u32((long long)N, a.bmax[2], 1u, sm, s);
-    }
+    if (e == cudaSuccess && a.group == 1) launch_attr_init(a, (long long)N, sm, s);
     return e;
 }
 

@@ -246,8 +246,27 @@ void launch_fill_u32(long long n, uint32_t *dst, uint32_t v, int sm, cudaStream_
     k_fill_u32<<<grid_for(n, 256, sm), 256, 0, s>>>(n, dst, v); note_launch();
 }
 
+// start values of the extent group's interleaved records (two 16-byte stores each):
+// area and pending 0, bounding-box minima all-ones, maxima 0; in 2-D every pixel has
+// z = 0, so the z extent is the fixed [0, 1)
+__global__ void k_attr_init_extent(long long n, uint4 *rec, bool has_z)
+{
+    const uint4 lo = make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    const uint4 hi = has_z ? make_uint4(0xFFFFFFFFu, 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, 1u);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        rec[2 * i] = lo;
+        rec[2 * i + 1] = hi;
+    }
+}
+
+void launch_attr_init(const AttrBufs &a, long long n, int sm, cudaStream_t s)
+{
+    if (a.group != 1) return;  // the other groups start at zero (the caller's memset)
+    k_attr_init_extent<<<grid_for(n, 256, sm), 256, 0, s>>>(n, (uint4 *)a.area.p, a.has_z); note_launch();
+}
+
 // leaves get pending = -1; nodes with exactly one child are flagged in `single`
-__global__ void k_mark_leaves(const int *__restrict__ nodes, const unsigned long long *num_nodes, int *pending,
+__global__ void k_mark_leaves(const int *__restrict__ nodes, const unsigned long long *num_nodes, Field<int> pending,
                               unsigned char *single)
 {
     NODE_LOOP(p, nodes, num_nodes)
@@ -269,12 +288,19 @@ struct Rec {
 template <int G, bool EXACT>
 __device__ __forceinline__ void rec_load(const AttrBufs &a, int u, Rec<G, EXACT> &r)
 {
+    if (G == 1) {  // the whole interleaved record (REC1_WORDS words) in two 16-byte loads
+        const uint4 *rp = (const uint4 *)(a.area + u);
+        const uint4 r0 = __ldcg(rp), r1 = __ldcg(rp + 1);
+        r.area = r0.x;
+        r.bmin[0] = r0.z;
+        r.bmin[1] = r0.w;
+        r.bmin[2] = r1.x;
+        r.bmax[0] = r1.y;
+        r.bmax[1] = r1.z;
+        r.bmax[2] = r1.w;
+        return;
+    }
     r.area = __ldcg(a.area + u);
-    if (G == 1)
-        for (int d = 0; d < 3; d++) {
-            r.bmin[d] = __ldcg(a.bmin[d] + u);
-            r.bmax[d] = __ldcg(a.bmax[d] + u);
-        }
     if (G == 2 || G == 4)
         for (int d = 0; d < 3; d++) r.s1[d] = s1_used(a, d) ? __ldcg(a.s1[d] + u) : 0ull;
     if (G == 4)
@@ -288,6 +314,20 @@ __device__ __forceinline__ void rec_load(const AttrBufs &a, int u, Rec<G, EXACT>
 template <int G, bool EXACT>
 __device__ __forceinline__ void rec_absorb_store(const AttrBufs &a, int q, Rec<G, EXACT> &r)
 {
+    if (G == 1) {  // load, combine and store the interleaved record whole; pending is cleared
+        uint4 *rp = (uint4 *)(a.area + q);
+        const uint4 q0 = __ldcg(rp), q1 = __ldcg(rp + 1);
+        r.area += q0.x;
+        r.bmin[0] = min(r.bmin[0], q0.z);
+        r.bmin[1] = min(r.bmin[1], q0.w);
+        r.bmin[2] = min(r.bmin[2], q1.x);
+        r.bmax[0] = max(r.bmax[0], q1.y);
+        r.bmax[1] = max(r.bmax[1], q1.z);
+        r.bmax[2] = max(r.bmax[2], q1.w);
+        __stcg(rp, make_uint4(r.area, 0u, r.bmin[0], r.bmin[1]));
+        __stcg(rp + 1, make_uint4(r.bmin[2], r.bmax[0], r.bmax[1], r.bmax[2]));
+        return;
+    }
     r.area += __ldcg(a.area + q);
     __stcg(a.area + q, r.area);
     if (G == 1)
@@ -390,7 +430,7 @@ __global__ void k_attr_up(const int *__restrict__ nodes, const unsigned long lon
 
 // nodes left for the pointer-jumping phase, listed in any order
 // (list entries beyond cap are dropped and flagged: the caller sized the list)
-__global__ void k_collect_rest(const int *__restrict__ nodes, const unsigned long long *num_nodes, int *pending,
+__global__ void k_collect_rest(const int *__restrict__ nodes, const unsigned long long *num_nodes, Field<int> pending,
                                int *list, unsigned *count, unsigned cap, unsigned *err)
 {
     NODE_LOOP(p, nodes, num_nodes)
@@ -446,7 +486,7 @@ __device__ __forceinline__ void rest_copy(const RestRecs &dst, int i, const Attr
 
 template <int G>
 __global__ void k_rest_gather(const int *__restrict__ list, const unsigned *count, unsigned cap,
-                              const int *__restrict__ parent, int *pending, AttrBufs a, RestRecs r, int *jump,
+                              const int *__restrict__ parent, Field<int> pending, AttrBufs a, RestRecs r, int *jump,
                               unsigned *err)
 {
     const unsigned R = rest_count(count, cap);
@@ -458,7 +498,7 @@ __global__ void k_rest_gather(const int *__restrict__ list, const unsigned *coun
 
 template <int G>
 __global__ void k_rest_links(const int *__restrict__ list, const unsigned *count, unsigned cap,
-                             const int *__restrict__ parent, const int *__restrict__ pending, int *jump, unsigned *err)
+                             const int *__restrict__ parent, Field<int> pending, int *jump, unsigned *err)
 {
     const unsigned R = rest_count(count, cap);
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {

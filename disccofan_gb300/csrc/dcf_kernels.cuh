@@ -146,22 +146,41 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
 long long batch_seam_edge_bound(const Geom &bg, const BatchImg *imgs_host, int count);
 
 // ---------------------------------------------------------------------------
-// attribute records (structure of arrays over pixels; valid at level roots)
+// attribute records (indexed by pixel; valid at level roots)
 // ---------------------------------------------------------------------------
+// One 32-bit field of the records: element i at p[i * stride].  The 32-bit fields of
+// a node are interleaved so that a pass touching one node's record reads one
+// 32-byte sector instead of one sector per field: in the extent group the record
+// is REC1_WORDS words (area, pending, bmin x/y/z, bmax x/y/z), in the other groups
+// area and pending share one 8-byte pair.  The 64-bit moment sums stay one array
+// per field.
+template <typename T>
+struct Field {
+    T *p = nullptr;
+    int stride = 1;
+    __host__ __device__ T &operator[](long long i) const { return p[i * stride]; }
+    __host__ __device__ T *operator+(long long i) const { return p + i * stride; }
+};
+constexpr int REC1_WORDS = 8;  // extent-group record: area, pending, bmin[3], bmax[3]
+
 struct AttrBufs {
     int group = -1;
     bool exact_g = false;            // grey-weighted sums kept as exact integers (u8/u16)
     bool has_z = true;               // 3-D image: z extent is accumulated (2-D: fixed [0,1))
-    uint32_t *area = nullptr;
-    uint32_t *bmin[3] = {nullptr, nullptr, nullptr};
-    uint32_t *bmax[3] = {nullptr, nullptr, nullptr};
+    Field<uint32_t> area;
+    Field<uint32_t> bmin[3];
+    Field<uint32_t> bmax[3];
     unsigned long long *s1[3] = {nullptr, nullptr, nullptr};   // sum x, y, z
     unsigned long long *s2[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // x2 y2 z2 xy yz xz
     void *gw[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // sum g, g^2, g*x, g*y, g*z (i64 or f64)
-    int *pending = nullptr;          // children not yet folded in (bottom-up pass)
+    Field<int> pending;              // children not yet folded in (bottom-up pass)
     unsigned char *single = nullptr; // node has exactly one child (bottom-up pass)
     bool grey = true;                // inertia group: accumulate the grey-weighted sums too
 };
+
+// every record of `a` over n pixels set to its start value: zero sums, empty
+// bounding boxes (minimum all-ones), and in 2-D the fixed z extent [0, 1)
+void launch_attr_init(const AttrBufs &a, long long n, int sm_count, cudaStream_t s);
 
 // Fields a pass must move: z moments only in 3-D; grey-weighted sums for the wmean
 // group, and for the inertia group only when asked (its attributes 13-17 use the
