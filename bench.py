@@ -193,26 +193,38 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    # a dedicated stream: the library's kernels and the timing events share it
-    stream = torch.cuda.Stream()
+    # a dedicated stream per tree: the step's max and min trees are independent, so
+    # they run concurrently, one library context (stream) and one host thread each
+    # (--serial-trees: one after the other on one stream); the timing events are on
+    # the first stream, which joins the second at the end of the timed region
+    from concurrent.futures import ThreadPoolExecutor
+    concurrent = not args.serial_trees
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    stream = streams[0]
     torch.cuda.set_stream(stream)
-    ctx = dcf.Context(local, stream=stream.cuda_stream)
+    ctxs = [dcf.Context(local, stream=s.cuda_stream) for s in streams]
+    ctx = ctxs[0]
+    pool = ThreadPoolExecutor(2)
     size = args.size
     img = make_image(size, seed=2 + rank)
     npix = size * size
     l_elong, l_area = lvecs(npix)
     d_out = [torch.empty(npix, dtype=torch.float32, device="cuda") for _ in range(2)]
     d_spec = [torch.zeros((l_area.size, l_elong.size), dtype=torch.float64, device="cuda") for _ in range(2)]
+    TREES = ("max", "min")
 
-    def step():
-        nodes = []
-        for k, tt in enumerate(("max", "min")):
-            t = ctx.build(img, connectivity=8, tree_type=tt, attribute=18)
+    def tree_work(k, c, src):
+        with torch.cuda.stream(streams[k] if c is ctxs[k] else stream):
+            t = c.build(src, connectivity=8, tree_type=TREES[k], attribute=18)
             t.filter(0, 1000.0, "direct", out=d_out[k])
             d_spec[k].zero_()
             t.pattern_spectrum2d(18, l_elong, 0, l_area, out=d_spec[k])
-            nodes.append(t)
-        return nodes
+        return t
+
+    def step(conc=concurrent):
+        if conc:
+            return [f.result() for f in [pool.submit(tree_work, k, ctxs[k], img) for k in range(2)]]
+        return [tree_work(k, ctx, img) for k in range(2)]
 
     def barrier():
         torch.cuda.synchronize()
@@ -222,28 +234,36 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         step()
-    ctx.synchronize()
+    barrier()
     info_trees = step()
     node_counts = [t.info()["nodes"] for t in info_trees]
     del info_trees
     barrier()
 
-    # device-resident timed region (with per-kernel CUDA events on the same stream)
-    ctx.set_profiling(True)
-    launches0 = ctx.launches
+    # device-resident timed region
+    launches0 = sum(c.launches for c in ctxs)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier()
         ev0.record(stream)
+        streams[1].wait_event(ev0)
         for _ in range(args.steps):
             step()
+        stream.wait_stream(streams[1])
         ev1.record(stream)
         barrier()
     ms = ev0.elapsed_time(ev1) / args.steps
-    launches = ctx.launches - launches0
+    launches = sum(c.launches for c in ctxs) - launches0
+    # per-kernel split: CUDA events on one stream over serial steps (the concurrent
+    # steps overlap kernels of the two trees, so per-kernel times would overlap too)
+    prof_steps = max(1, min(args.steps, 3))
+    ctx.set_profiling(True)
+    for _ in range(prof_steps):
+        step(conc=False)
     prof = ctx.profile()
     ctx.set_profiling(False)
     ctx.synchronize()
+    prof_ms_step = sum(v[0] for v in prof.values()) / prof_steps
 
     # e2e through the public API: the pinned host image is staged on the device once
     # per step (dcf_image_stage) for both trees; the filtered images come back in
@@ -256,14 +276,22 @@ def run_ours(args):
                          pin_memory=True).numpy().view(np.uint16) for _ in range(2)]
     h_spec = [np.zeros((l_area.size, l_elong.size), np.float64) for _ in range(2)]
 
+    def e2e_tree(k, c, staged):
+        t = c.build(staged, connectivity=8, tree_type=TREES[k], attribute=18)
+        t.filter(0, 1000.0, "direct", out=h_out[k])
+        h_spec[k][:] = 0
+        t.pattern_spectrum2d(18, l_elong, 0, l_area, out=h_spec[k])
+        t.close()
+
     def e2e_step():
         staged = ctx.stage(h_img_np)
-        for k, tt in enumerate(("max", "min")):
-            t = ctx.build(staged, connectivity=8, tree_type=tt, attribute=18)
-            t.filter(0, 1000.0, "direct", out=h_out[k])
-            h_spec[k][:] = 0
-            t.pattern_spectrum2d(18, l_elong, 0, l_area, out=h_spec[k])
-            t.close()
+        if concurrent:
+            ctx.synchronize()  # the staged copy is read from the second context's stream too
+            for f in [pool.submit(e2e_tree, k, ctxs[k], staged) for k in range(2)]:
+                f.result()
+        else:
+            for k in range(2):
+                e2e_tree(k, ctx, staged)
 
     e2e_step()
     barrier()
@@ -342,7 +370,10 @@ def run_ours(args):
                                          "traffic_ratio": None if pipeline_traffic is None else
                                          round(pipeline_traffic / B_alg, 3),
                                          "dram_source": dram["source"] if dram else None},
-                   "kernel_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sorted(prof.items())}},
+                   "trees": "concurrent (two contexts, two streams)" if concurrent else "serial (one stream)",
+                   "kernel_ms_per_step": {k: round(v[0] / prof_steps, 3) for k, v in sorted(prof.items())},
+                   "kernel_split": f"CUDA events on one stream over {prof_steps} serial steps "
+                                   f"({prof_ms_step:.1f} ms/step of kernels)"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": traffic,
                      "traffic_source": None if traffic is None else
@@ -763,6 +794,8 @@ def main():
     ap.add_argument("--ref-reps", type=int, default=1, help="--impl reference: full-size steps timed")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
+    ap.add_argument("--serial-trees", action="store_true",
+                    help="build a step's max and min trees one after the other on one stream")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-cutout workload")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint workload")
     ap.add_argument("--no-autotune", action="store_true", help="batched workload: keep the default schedule")
