@@ -39,7 +39,9 @@ struct dcf_ctx {
     char last_error[512] = {0};
     uint64_t launches = 0;
     int up_steps = 2048;              // bottom-up fold steps per walker before pointer jumping
-    int tile2d[2] = {64, 64};         // build tile of 2-D images (width, height)
+    // build tile of 2-D images (width, height): 128 x 32 builds faster than 64 x 64
+    // (fewer band-merge levels) at the price of more seam edges
+    int tile2d[2] = {128, 32};
     int tile3d[3] = {16, 16, 16};     // build tile of 3-D images
     int level_sync = 1;               // barrier between band-merge levels inside a tile
     // level buckets of the seam merge: 1 = every cross-tile edge at once, from a
