@@ -1131,8 +1131,9 @@ extern "C" dcf_status dcf_filter_direct_noalloc(dcf_ctx *ctx, dcf_tree *t, int a
     }
     ActiveScope active_scope_(ctx);
     // layout: N resolved-node indices (int32), then N survive bytes; every call
-    // rewrites both for all pixels (k_flag resets the indices), so nothing carries
-    // over from the previous call
+    // rewrites both at every level root of the tree (k_flag resets the indices),
+    // the only entries the filter passes read, so nothing carries over from the
+    // previous call
     FilterWork w{};
     w.target = (int *)base;
     w.flag = (unsigned char *)base + (size_t)NOALLOC_MAX_PIXELS * 4;

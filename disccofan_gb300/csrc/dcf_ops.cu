@@ -28,14 +28,17 @@ constexpr int UNKNOWN = -2;
 #define GRID_LOOP(p, n) \
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < (n); p += (long long)gridDim.x * blockDim.x)
 
+// presolve (direct rule): a surviving node is its own resolution, so k_resolve<.., true>
+// walks on `target` alone
 __global__ void k_flag(Geom g, NodeSet ns, AttrBufs a, int attr, double lambda,
-                       float pd0, float pd1, float pd2, unsigned char *flag, int *target)
+                       float pd0, float pd1, float pd2, unsigned char *flag, int *target, bool presolve)
 {
     const float pd[3] = {pd0, pd1, pd2};
     NODE_LOOP(p, ns.nodes, ns.num)
     {
-        target[p] = UNKNOWN;
-        flag[p] = attr_value(a, attr, (int)p, pd) >= lambda ? 1 : 0;
+        const bool keep = attr_value(a, attr, (int)p, pd) >= lambda;
+        target[p] = presolve && keep ? p : UNKNOWN;
+        flag[p] = keep ? 1 : 0;
     }
 }
 
@@ -56,7 +59,8 @@ __global__ void k_mark_kept(Geom g, NodeSet ns, const int *__restrict__ parent,
 }
 
 // nearest flagged ancestor-or-self; flag may be a byte array or the kept words
-template <typename F>
+// (PRESOLVED: the flagged nodes already hold themselves in target; flag unused)
+template <typename F, bool PRESOLVED>
 __global__ void k_resolve(Geom g, NodeSet ns, const int *__restrict__ parent,
                           const F *__restrict__ flag, int *target, unsigned *err)
 {
@@ -68,7 +72,7 @@ __global__ void k_resolve(Geom g, NodeSet ns, const int *__restrict__ parent,
         for (; it < g.N; it++) {
             int t = ((volatile int *)target)[v];
             if (t != UNKNOWN) { res = t; break; }
-            if (flag[v]) { res = v; break; }
+            if (!PRESOLVED && flag[v]) { res = v; break; }
             int q = parent[v];
             if (q == NONE) { res = NONE; break; }
             v = q;
@@ -244,16 +248,16 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
     k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
-                              w.target); note_launch();
+                              w.target, rule == 0); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
     const double *accp = nullptr;
     if (rule == 0) {
-        k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
+        k_resolve<unsigned char, true><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
     } else if (rule == 2) {
         cudaMemsetAsync(w.kept, 0, t.g.N * sizeof(unsigned), s);
         k_mark_kept<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.kept, err); note_launch();
-        k_resolve<unsigned><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.kept, w.target, err); note_launch();
+        k_resolve<unsigned, false><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.kept, w.target, err); note_launch();
     } else {
         const int R = rounds_for(depth_bound);
         int *j0 = w.jump, *j1 = w.jump2;
@@ -817,10 +821,10 @@ void launch_direct_targets(const TreeView &t, const AttrBufs &a, int attr, doubl
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
     k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
-                              w.target); note_launch();
+                              w.target, true); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(P_RESOLVE, s);
-    k_resolve<unsigned char><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
+    k_resolve<unsigned char, true><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
     prof_end(P_RESOLVE, s);
 }
 
