@@ -785,26 +785,51 @@ int64_t dco_aux(const dco_tree *t, void *out, uint64_t out_bytes)
 
 #define AV(t, a, i) attr_value((t), (a), ATTR((t), (i)))
 
+/* The threads filter disjoint pixel ranges but stop at, and read, nodes that other
+ * threads have already resolved.  The reference (filtering.c:55-261) shares out[]
+ * and reached[] through plain loads and stores, and its min rule sets reached[]
+ * before out[]; on Arm's weakly ordered memory a reader can then see reached[w]
+ * set while out[w] still holds the zero it was cleared to, and copy that zero
+ * down its path.  Here out[u] is published by a release store of reached[u] and
+ * read only after an acquire load of it, which are plain loads and stores on x86
+ * (the results there are the reference's).  reached[] is only ever raised, except
+ * where the max rule lowers another range's entry as the reference does (:182). */
+static inline bool seen(const bool *reached, idx_t i) { return __atomic_load_n(&reached[i], __ATOMIC_ACQUIRE); }
+
+static inline void publish(float *out, bool *reached, idx_t i, float v)
+{
+    __atomic_store(&out[i], &v, __ATOMIC_RELAXED);
+    __atomic_store_n(&reached[i], true, __ATOMIC_RELEASE);
+}
+
+/* out[] of another range read without reached[] (the max rule's climb, :177) */
+static inline float peek(const float *out, idx_t i)
+{
+    float v;
+    __atomic_load(&out[i], &v, __ATOMIC_RELAXED);
+    return v;
+}
+
 /* tree_filter_direct (filtering.c:102-154) */
 static void filter_direct(dco_tree *t, float *out, bool *reached, uint64_t lwb, uint64_t upb, int a, double lambda)
 {
     for (uint64_t v = lwb; v < upb; v++) {
-        if (reached[v]) continue;
+        if (seen(reached, (idx_t)v)) continue;
         idx_t w = (idx_t)v, par = t->parent[w];
-        while (par != BOTTOM && !reached[w] && (t->gval[w] == t->gval[par] || AV(t, a, w) < lambda)) {
+        while (par != BOTTOM && !seen(reached, w) && (t->gval[w] == t->gval[par] || AV(t, a, w) < lambda)) {
             w = par;
             par = t->parent[w];
         }
         float val;
-        if (reached[w]) val = out[w];
+        if (seen(reached, w)) val = out[w];
         else if (AV(t, a, w) >= lambda) val = t->gval[w];
         else val = 0;
         idx_t u = (idx_t)v;
         while (u != w) {
-            if ((uint64_t)u >= lwb && (uint64_t)u < upb) { out[u] = val; reached[u] = true; }
+            if ((uint64_t)u >= lwb && (uint64_t)u < upb) publish(out, reached, u, val);
             u = t->parent[u];
         }
-        if ((uint64_t)w >= lwb && (uint64_t)w < upb) { out[w] = val; reached[w] = true; }
+        if ((uint64_t)w >= lwb && (uint64_t)w < upb) publish(out, reached, w, val);
     }
 }
 
@@ -812,15 +837,15 @@ static void filter_direct(dco_tree *t, float *out, bool *reached, uint64_t lwb, 
 static void filter_min(dco_tree *t, float *out, bool *reached, uint64_t lwb, uint64_t upb, int a, double lambda)
 {
     for (uint64_t v = lwb; v < upb; v++) {
-        if (reached[v]) continue;
+        if (seen(reached, (idx_t)v)) continue;
         idx_t w = levelroot(t, (idx_t)v), r = w, par = get_parent(t, w);
-        while (par != BOTTOM && !reached[w]) {
+        while (par != BOTTOM && !seen(reached, w)) {
             if (AV(t, a, w) < lambda) r = w;
             w = par;
             par = get_parent(t, w);
         }
         float val;
-        if (reached[w] && out[w] != t->gval[w]) {
+        if (seen(reached, w) && out[w] != t->gval[w]) {
             val = out[w];
             r = w;
         } else if (AV(t, a, r) >= lambda) {
@@ -832,10 +857,10 @@ static void filter_min(dco_tree *t, float *out, bool *reached, uint64_t lwb, uin
         }
         idx_t u = (idx_t)v;
         while (u != r) {
-            if ((uint64_t)u >= lwb && (uint64_t)u < upb) { reached[u] = true; out[u] = val; }
+            if ((uint64_t)u >= lwb && (uint64_t)u < upb) publish(out, reached, u, val);
             u = t->parent[u];
         }
-        if ((uint64_t)r >= lwb && (uint64_t)r < upb) { reached[r] = true; out[r] = val; }
+        if ((uint64_t)r >= lwb && (uint64_t)r < upb) publish(out, reached, r, val);
     }
 }
 
@@ -843,24 +868,23 @@ static void filter_min(dco_tree *t, float *out, bool *reached, uint64_t lwb, uin
 static void filter_max(dco_tree *t, float *out, bool *reached, uint64_t lwb, uint64_t upb, int a, double lambda)
 {
     for (uint64_t v = lwb; v < upb; v++) {
-        if (reached[v]) continue;
+        if (seen(reached, (idx_t)v)) continue;
         idx_t w = (idx_t)v, par = t->parent[w], u;
-        while (par != BOTTOM && !reached[w] && (t->gval[w] == t->gval[par] || AV(t, a, w) < lambda)) {
+        while (par != BOTTOM && !seen(reached, w) && (t->gval[w] == t->gval[par] || AV(t, a, w) < lambda)) {
             w = par;
             par = t->parent[w];
         }
         float val;
-        if (reached[w]) {
+        if (seen(reached, w)) {
             val = out[w];
         } else if (AV(t, a, w) >= lambda) {
             val = t->gval[w];
             u = par;
-            while (u != BOTTOM && out[u] != t->gval[u]) {
+            while (u != BOTTOM && peek(out, u) != t->gval[u]) {
                 if ((uint64_t)u >= lwb && (uint64_t)u < upb) {
-                    out[u] = t->gval[u];
-                    reached[u] = true;
+                    publish(out, reached, u, t->gval[u]);
                 } else {
-                    reached[u] = false;
+                    __atomic_store_n(&reached[u], false, __ATOMIC_RELAXED);
                     break;
                 }
                 u = t->parent[u];
@@ -870,10 +894,10 @@ static void filter_max(dco_tree *t, float *out, bool *reached, uint64_t lwb, uin
         }
         u = (idx_t)v;
         while ((uint64_t)u != (uint64_t)w) {
-            if ((uint64_t)u >= lwb && (uint64_t)u < upb) { out[u] = val; reached[u] = true; }
+            if ((uint64_t)u >= lwb && (uint64_t)u < upb) publish(out, reached, u, val);
             u = t->parent[u];
         }
-        if ((uint64_t)w >= lwb && (uint64_t)w < upb) { out[w] = val; reached[w] = true; }
+        if ((uint64_t)w >= lwb && (uint64_t)w < upb) publish(out, reached, w, val);
     }
 }
 
@@ -885,10 +909,10 @@ static void filter_subtractive(dco_tree *t, float *out, bool *reached, uint64_t 
     idx_t *levpath = malloc(t->max_levels * sizeof(idx_t));
     float *filt = malloc(t->max_levels * sizeof(float));
     for (uint64_t v = lwb; v < upb; v++) {
-        if (reached[v]) continue;
+        if (seen(reached, (idx_t)v)) continue;
         idx_t w = levelroot(t, (idx_t)v), u;
         int64_t i = 0, j;
-        while (w != BOTTOM && !reached[w]) {
+        while (w != BOTTOM && !seen(reached, w)) {
             levpath[i++] = w;
             w = get_parent(t, w);
         }
@@ -909,10 +933,10 @@ static void filter_subtractive(dco_tree *t, float *out, bool *reached, uint64_t 
         u = (idx_t)v;
         for (j = 0; j <= i; j++) {
             while ((uint64_t)u != (uint64_t)levpath[j]) {
-                if ((uint64_t)u >= lwb && (uint64_t)u < upb) { out[u] = filt[j]; reached[u] = true; }
+                if ((uint64_t)u >= lwb && (uint64_t)u < upb) publish(out, reached, u, filt[j]);
                 u = t->parent[u];
             }
-            if ((uint64_t)u >= lwb && (uint64_t)u < upb) { out[u] = filt[j]; reached[u] = true; }
+            if ((uint64_t)u >= lwb && (uint64_t)u < upb) publish(out, reached, u, filt[j]);
             if (u != BOTTOM) u = t->parent[u];
         }
     }

@@ -190,6 +190,38 @@ def test_random_against_oracle(ctx, shape, kind, conn, tree):
             np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12 * np.abs(want).max(), err_msg=str((a1, a2)))
 
 
+def smooth_u16(rng, n):
+    """Low-pass noise on 0..40000: level components of thousands of pixels that
+    cross every slab seam of a multi-threaded build and filter."""
+    f = np.fft.rfft2(rng.standard_normal((n, n)))
+    ky = np.fft.fftfreq(n)[:, None]
+    kx = np.fft.rfftfreq(n)[None, :]
+    f *= np.exp(-(kx ** 2 + ky ** 2) * (n / 24.0) ** 2)
+    s = np.fft.irfft2(f, (n, n))
+    s = (s - s.min()) / (s.max() - s.min())
+    return (s * 40000).astype(np.uint16)
+
+
+@pytest.mark.parametrize("tree", ["max", "min"])
+def test_threaded_oracle_filters_agree_with_gpu(ctx, tree):
+    # The oracle's filter threads read nodes other threads resolved; that exchange is
+    # ordered (release/acquire), so on this host's weakly ordered cores too the
+    # threaded port equals its single-threaded self and the GPU, rules 0, 1 and 3
+    import os
+    img = smooth_u16(np.random.default_rng(5), 1024)
+    nt = max(8, os.cpu_count() or 1)
+    one, many = oracle.Port(threads=1), oracle.Port(threads=nt)
+    one.load(img.astype(np.float32), 8, tree, threads=1)
+    many.load(img.astype(np.float32), 8, tree, threads=nt)
+    t = gpu_tree(ctx, img, 8, tree)
+    for rule in (0, 1, 3):
+        for lam in (100.0, 5000.0):
+            ref = one.filter(0, lam, rule)
+            got = many.filter(0, lam, rule)
+            assert np.array_equal(got, ref), (rule, lam, int((got != ref).sum()))
+            assert np.array_equal(t.filter(0, lam, rule), ref), (rule, lam)
+
+
 @pytest.mark.parametrize("kind,conn,tree", [("u8", 4, "max"), ("u16", 8, "min"), ("u16", 8, "max")])
 def test_filter_in_input_type_and_staged_builds(ctx, kind, conn, tree):
     # dcf_filter_as: every rule (and extract) in the input's own integer type equals
