@@ -17,6 +17,7 @@ importing this module fails loudly when the library has not been built.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import os
 
@@ -139,6 +140,8 @@ def library() -> C.CDLL:
     L.dcf_status_string.restype = C.c_char_p
     L.dcf_ctx_launch_count.argtypes = [vp]
     L.dcf_ctx_launch_count.restype = C.c_uint64
+    L.dcf_ctx_stream.argtypes = [vp]
+    L.dcf_ctx_stream.restype = C.c_void_p
     L.dcf_ctx_set_profiling.argtypes = [vp, i]
     L.dcf_ctx_set_profiling.restype = C.c_int
     L.dcf_ctx_profile.argtypes = [vp, i, C.POINTER(d), C.POINTER(u64)]
@@ -222,6 +225,31 @@ class Context:
             raise DcfError(st, "dcf_ctx_create")
         self.h = h
         self.device = device
+        self._torch_stream = None
+
+    @contextlib.contextmanager
+    def ordered(self, *arrays):
+        """Around a call that reads or writes CUDA tensors: this context's stream first
+        waits for the work queued on torch's current stream (the tensors' producers),
+        and torch's current stream then waits for the call (its consumers, and the
+        caching allocator's reuse of the tensors).  Nothing to do for host arrays, or
+        when torch's current stream is this context's stream."""
+        if not any(_is_torch_cuda(a) for a in arrays):
+            yield
+            return
+        import torch
+        cur = torch.cuda.current_stream(self.device)
+        if self._torch_stream is None:
+            self._torch_stream = torch.cuda.ExternalStream(self.lib.dcf_ctx_stream(self.h), device=self.device)
+        own = self._torch_stream
+        same = cur.cuda_stream == own.cuda_stream
+        if not same:
+            own.wait_stream(cur)
+        try:
+            yield
+        finally:
+            if not same:
+                cur.wait_stream(own)
 
     def close(self):
         if getattr(self, "h", None) and not _exiting:
@@ -341,7 +369,8 @@ class Tree:
         im = _Image(ptr, DTYPES[dt], int(on_dev), (C.c_uint64 * 3)(w, h, d), connectivity,
                     TREE_TYPES[tree_type], (C.c_float * 3)(*pixdim))
         hnd = C.c_void_p()
-        ctx.check(L.dcf_tree_build(ctx.h, C.byref(im), attribute, C.byref(hnd)), "dcf_tree_build")
+        with ctx.ordered(image):
+            ctx.check(L.dcf_tree_build(ctx.h, C.byref(im), attribute, C.byref(hnd)), "dcf_tree_build")
         self.h = hnd
         self.n = w * h * d
         self.attribute = attribute
@@ -405,19 +434,22 @@ class Tree:
     # -- tree data ---------------------------------------------------------
     def parent(self, out=None):
         a, p, dev = self._out(np.int64, out)
-        self.ctx.check(self.ctx.lib.dcf_tree_parent(self.ctx.h, self.h, p, dev), "parent")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_tree_parent(self.ctx.h, self.h, p, dev), "parent")
         return a
 
     def gval(self, out=None):
         a, p, dev = self._out(np.float32, out)
-        self.ctx.check(self.ctx.lib.dcf_tree_gval(self.ctx.h, self.h, p, dev), "gval")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_tree_gval(self.ctx.h, self.h, p, dev), "gval")
         return a
 
     def node_attribute(self, attribute: int, area: bool = False, out=None):
         self._ensure_group(attribute)
         a, p, dev = self._out(np.float64, out)
-        self.ctx.check(self.ctx.lib.dcf_node_attribute(self.ctx.h, self.h, attribute, int(area), p, dev),
-                       "node_attribute")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_node_attribute(self.ctx.h, self.h, attribute, int(area), p, dev),
+                           "node_attribute")
         return a
 
     # -- operations (operation.c) ------------------------------------------
@@ -435,21 +467,24 @@ class Tree:
                 out_dtype = np.uint8
         if out_dtype is None or np.dtype(out_dtype) == np.float32:
             a, p, dev = self._out(np.float32, out)
-            self.ctx.check(self.ctx.lib.dcf_filter(self.ctx.h, self.h, attribute, r, float(lam), int(extract), p,
-                                                   dev), "filter")
+            with self.ctx.ordered(a):
+                self.ctx.check(self.ctx.lib.dcf_filter(self.ctx.h, self.h, attribute, r, float(lam), int(extract), p,
+                                                       dev), "filter")
             return self._shape(a)
         odt = np.dtype(out_dtype)
         if odt not in DTYPES:
             raise TypeError(f"unsupported output dtype {odt}")
         a, p, dev = self._out(odt, out)
-        self.ctx.check(self.ctx.lib.dcf_filter_as(self.ctx.h, self.h, attribute, r, float(lam), int(extract),
-                                                  DTYPES[odt], p, dev), "filter_as")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_filter_as(self.ctx.h, self.h, attribute, r, float(lam), int(extract),
+                                                      DTYPES[odt], p, dev), "filter_as")
         return self._shape(a)
 
     def check(self, attribute: int, out=None):
         self._ensure_group(attribute)
         a, p, dev = self._out(np.float32, out)
-        self.ctx.check(self.ctx.lib.dcf_attribute_check(self.ctx.h, self.h, attribute, p, dev), "check")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_attribute_check(self.ctx.h, self.h, attribute, p, dev), "check")
         return self._shape(a)
 
     def dmp(self, attribute: int, lvec, rule="direct", out=None):
@@ -457,7 +492,9 @@ class Tree:
         lv = np.ascontiguousarray(lvec, np.float32)
         r = RULES[rule] if isinstance(rule, str) else int(rule)
         a, p, dev = self._out(np.float32, out, count=(lv.size - 1) * self.n)
-        self.ctx.check(self.ctx.lib.dcf_dmp(self.ctx.h, self.h, attribute, r, lv.ctypes.data, lv.size, p, dev), "dmp")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_dmp(self.ctx.h, self.h, attribute, r, lv.ctypes.data, lv.size, p, dev),
+                           "dmp")
         return self._shape(a, (lv.size - 1,))
 
     def pattern_spectrum(self, attribute: int, lvec, out=None):
@@ -467,8 +504,9 @@ class Tree:
         spec = out if out is not None else np.zeros(lv.size, np.float64)
         dev = int(_is_torch_cuda(spec))
         p = spec.data_ptr() if dev else spec.ctypes.data
-        self.ctx.check(self.ctx.lib.dcf_pattern_spectrum(self.ctx.h, self.h, attribute, lv.ctypes.data, lv.size, p,
-                                                         dev), "pattern_spectrum")
+        with self.ctx.ordered(spec):
+            self.ctx.check(self.ctx.lib.dcf_pattern_spectrum(self.ctx.h, self.h, attribute, lv.ctypes.data, lv.size,
+                                                             p, dev), "pattern_spectrum")
         return spec
 
     def pattern_spectrum2d(self, attr1: int, lvec1, attr2: int, lvec2, out=None):
@@ -479,8 +517,10 @@ class Tree:
         spec = out if out is not None else np.zeros((l2.size, l1.size), np.float64)
         dev = int(_is_torch_cuda(spec))
         p = spec.data_ptr() if dev else spec.ctypes.data
-        self.ctx.check(self.ctx.lib.dcf_pattern_spectrum2d(self.ctx.h, self.h, attr1, l1.ctypes.data, l1.size, attr2,
-                                                           l2.ctypes.data, l2.size, p, dev), "pattern_spectrum2d")
+        with self.ctx.ordered(spec):
+            self.ctx.check(self.ctx.lib.dcf_pattern_spectrum2d(self.ctx.h, self.h, attr1, l1.ctypes.data, l1.size,
+                                                               attr2, l2.ctypes.data, l2.size, p, dev),
+                           "pattern_spectrum2d")
         return spec
 
     # -- adjoint -------------------------------------------------------------
@@ -502,7 +542,9 @@ class Tree:
         v, vp = ptr(grad_filtered, np.float32)
         w, wp = ptr(grad_spectrum, np.float64)
         a, p, _ = self._out(np.float32, out)
-        self.ctx.check(self.ctx.lib.dcf_tree_adjoint(self.ctx.h, self.h, C.byref(ops), vp, wp, p, dev), "adjoint")
+        with self.ctx.ordered(a, grad_filtered, grad_spectrum):
+            self.ctx.check(self.ctx.lib.dcf_tree_adjoint(self.ctx.h, self.h, C.byref(ops), vp, wp, p, dev),
+                           "adjoint")
         return self._shape(a)
 
 
@@ -572,7 +614,9 @@ class Batch:
     def autotune(self, pixels, repeats: int = 3) -> float:
         p, dev = self._pixels(pixels)
         ms = C.c_double()
-        self.ctx.check(self.ctx.lib.dcf_batch_autotune(self.ctx.h, self.h, p, dev, repeats, C.byref(ms)), "autotune")
+        with self.ctx.ordered(pixels):
+            self.ctx.check(self.ctx.lib.dcf_batch_autotune(self.ctx.h, self.h, p, dev, repeats, C.byref(ms)),
+                           "autotune")
         return ms.value
 
     def run(self, pixels, filter_attr: int = -1, lam: float = 0.0, spectrum=None, use_graph: bool = True,
@@ -594,8 +638,9 @@ class Batch:
             s = spectra if spectra is not None else np.empty((self.count, ops.n2, ops.n1), np.float64)
         fp = (f.data_ptr() if odev else f.ctypes.data) if f is not None else None
         sp = (s.data_ptr() if odev else s.ctypes.data) if s is not None else None
-        self.ctx.check(self.ctx.lib.dcf_batch_run(self.ctx.h, self.h, p, pdev, C.byref(ops), fp, sp, odev),
-                       "batch_run")
+        with self.ctx.ordered(pixels, f, s):
+            self.ctx.check(self.ctx.lib.dcf_batch_run(self.ctx.h, self.h, p, pdev, C.byref(ops), fp, sp, odev),
+                           "batch_run")
         self._ops_keep = keep
         return f, s
 
@@ -603,16 +648,18 @@ class Batch:
         """Canonical parents, as indices inside each cutout (concatenated)."""
         a = out if out is not None else np.empty(self.n, np.int64)
         dev = int(_is_torch_cuda(a))
-        self.ctx.check(self.ctx.lib.dcf_batch_parent(self.ctx.h, self.h, a.data_ptr() if dev else a.ctypes.data, dev),
-                       "batch_parent")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_batch_parent(self.ctx.h, self.h, a.data_ptr() if dev else a.ctypes.data,
+                                                         dev), "batch_parent")
         return a
 
     def node_attribute(self, attribute: int, out=None):
         a = out if out is not None else np.empty(self.n, np.float64)
         dev = int(_is_torch_cuda(a))
-        self.ctx.check(self.ctx.lib.dcf_batch_node_attribute(self.ctx.h, self.h, attribute,
-                                                             a.data_ptr() if dev else a.ctypes.data, dev),
-                       "batch_node_attribute")
+        with self.ctx.ordered(a):
+            self.ctx.check(self.ctx.lib.dcf_batch_node_attribute(self.ctx.h, self.h, attribute,
+                                                                 a.data_ptr() if dev else a.ctypes.data, dev),
+                           "batch_node_attribute")
         return a
 
     def adjoint(self, grad_filtered=None, grad_spectra=None, out=None):
@@ -630,5 +677,6 @@ class Batch:
             wp = w.ctypes.data if w is not None else None
             g = np.empty(self.n, np.float32)
             gp = g.ctypes.data
-        self.ctx.check(self.ctx.lib.dcf_batch_adjoint(self.ctx.h, self.h, vp, wp, gp, dev), "batch_adjoint")
+        with self.ctx.ordered(g, grad_filtered, grad_spectra):
+            self.ctx.check(self.ctx.lib.dcf_batch_adjoint(self.ctx.h, self.h, vp, wp, gp, dev), "batch_adjoint")
         return g

@@ -342,6 +342,8 @@ const char *dcf_ctx_last_error(const dcf_ctx *ctx) { return ctx ? ctx->last_erro
 
 uint64_t dcf_ctx_launch_count(const dcf_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+void *dcf_ctx_stream(const dcf_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
 dcf_status dcf_ctx_set_profiling(dcf_ctx *ctx, int enable)
 {
     if (!ctx) return DCF_ERR_INVALID;

@@ -59,6 +59,23 @@ k_batch_tile_build(const T *__restrict__ img, Geom bg, const BatchImg *__restric
     }
 }
 
+// the largest shared-memory split of the SM for the tile kernels (once per process)
+static void batch_tile_carveout()
+{
+    static bool done = (cudaFuncSetAttribute(k_batch_tile_build<uint8_t>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared),
+                        cudaFuncSetAttribute(k_batch_tile_build<uint16_t>,
+                                             cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared),
+                        cudaFuncSetAttribute(k_batch_tile_build<uint32_t>,
+                                             cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared),
+                        cudaFuncSetAttribute(k_batch_tile_build<float>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared),
+                        true);
+    (void)done;
+}
+
 // Seam edges of a batch: work item = (tile, face, face pixel, forward offset) over
 // the tile's +x, -x and +y faces; face f takes the offsets pointing out through
 // it.  2-D forward offsets never point to -y, so every edge between two tiles of
@@ -283,6 +300,7 @@ void launch_batch_build(int dtype, const void *img, const Geom &bg, const BatchI
                         int ctas_per_sm, SeamEdges &seam, int sm, cudaStream_t s)
 {
     const int grid = sm * ctas_per_sm;
+    batch_tile_carveout();
     cudaMemsetAsync(next, 0, sizeof(unsigned), s);
     prof_begin(P_TILE, s);
 #define DCF_TB(T)                                                                                       \
@@ -353,9 +371,11 @@ void launch_batch_spectrum(const Geom &bg, const BatchImg *imgs, const BatchTile
 
 namespace dcf {
 
-// CTAs of the persistent tile kernel that fit on one SM for a tile shape
+// CTAs of the persistent tile kernel that fit on one SM for a tile shape (with the
+// largest shared-memory split, which launch_batch_build asks for too)
 int batch_max_ctas_per_sm(int dtype, int tw, int th)
 {
+    batch_tile_carveout();
     int n = 0;
 #define DCF_OCC(T)                                                                                       \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_tile_build<T>, TileCfg<T>::threads,      \

@@ -437,6 +437,12 @@ static void build_t(const BuildArgs &a, cudaStream_t s)
     const int TW = a.g.tw, TH = a.g.th, TD = a.g.td;
     dim3 grid((a.g.W + TW - 1) / TW, (a.g.H + TH - 1) / TH, (a.g.D + TD - 1) / TD);
     const size_t smem = tile_smem_bytes(TW, TH, TD, TileCfg<T>::word_bytes);
+    // the largest shared-memory split of the SM, so the register file alone bounds
+    // the resident tiles (set once per instantiation)
+    static bool carveout = (cudaFuncSetAttribute(k_tile_build<T, MIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                 cudaSharedmemCarveoutMaxShared),
+                            true);
+    (void)carveout;
     prof_begin(P_TILE, s);
     k_tile_build<T, MIN><<<grid, TileCfg<T>::threads, smem, s>>>(img, a.g, a.kmax, a.gval, a.node, a.err); note_launch();
     prof_end(P_TILE, s);

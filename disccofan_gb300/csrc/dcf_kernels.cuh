@@ -31,19 +31,20 @@ __host__ __device__ inline long long merge_bound_global(const Geom &g)
     return g.merge_bound > 0 ? g.merge_bound : MERGE_BOUND_GLOBAL;
 }
 
-// dynamic shared memory of one tile build (padded node words + padded row stacks);
-// word_bytes 8 (u32/f32 images) or 4 (u8/u16: 16-bit level and parent)
+// dynamic shared memory of one tile build (padded node words); word_bytes 8
+// (u32/f32 images) or 4 (u8/u16: 16-bit level and parent)
 inline size_t tile_smem_bytes(int tw, int th, int td, int word_bytes = 8)
 {
-    return (size_t)(tw + 1) * th * td * word_bytes + (size_t)(tw + 2) * th * td * 2;
+    return (size_t)(tw + 1) * th * td * word_bytes;
 }
 // launch shape of the tile kernels per pixel type: u8/u16 tiles use 32-bit shared
-// words and 128-thread CTAs (25 KB for 64x64: 8 resident per SM), u32/f32 tiles
-// 64-bit words and 256 threads (42 KB: 5 per SM)
+// words and 128-thread CTAs (16.5 KB for 4096 pixels: 12 resident per SM, the
+// register file's limit at 40 registers a thread), u32/f32 tiles 64-bit words and
+// 256 threads (33 KB; 5 per SM, where they run without register spills)
 template <typename T> struct TileCfg {
     static constexpr bool narrow = sizeof(T) <= 2;
     static constexpr int threads = narrow ? TILE_THREADS_NARROW : TILE_THREADS;
-    static constexpr int min_blocks = narrow ? 8 : 5;
+    static constexpr int min_blocks = narrow ? 12 : 5;
     static constexpr int word_bytes = narrow ? 4 : 8;
 };
 

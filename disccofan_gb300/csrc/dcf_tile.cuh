@@ -119,10 +119,12 @@ __device__ __forceinline__ void connect_s(SmemAcc<W> &acc, int a, int b, long lo
 // (off > 0 for one cutout of a batch).  Writes gval and the tile forest
 // (level-root form, global indices, 64-bit order-key words) into gnode.
 //
-// Shared-memory layout (tile_smem_bytes): node words with a padded row stride
-// RS = tw + 1 (local index of pixel (lx, ly, lz) = lx + ly*RS + lz*RS*th), then one
-// stack per row with stride tw + 2 entries.  The row pass runs one row per thread
-// in lock-step; unpadded strides would put the rows of a warp in one bank.
+// Shared-memory layout (tile_smem_bytes): the node words alone, with a padded row
+// stride RS = tw + 1 (local index of pixel (lx, ly, lz) = lx + ly*RS + lz*RS*th).
+// The row pass runs one row per thread in lock-step; unpadded strides would put the
+// rows of a warp in one bank.  Nothing else is staged: the row stacks live in the
+// parent fields and the level-root form is made in place, so a tile of 4096 u8/u16
+// pixels takes 16.5 KB and 12 tiles are resident per SM (8 with a stack array).
 template <typename T, bool MIN>
 __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long off, const Geom &g, int x0, int y0,
                                            int z0, float gmax, float *__restrict__ gval,
@@ -134,9 +136,8 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     // tile extents from the geometry (at most 4096 pixels: local indices < 2^16)
     const bool is3d = g.D > 1;
     const int TW = g.tw, TH = g.th, TD = g.td;
-    const int RS = TW + 1, SS = TW + 2, SLICE = RS * TH, WORDS = RS * TH * TD;
-    WT *snode = (WT *)smem_raw;                                        // WORDS node words
-    unsigned short *sstk = (unsigned short *)(snode + WORDS);          // one stack per row
+    const int RS = TW + 1, SLICE = RS * TH, WORDS = RS * TH * TD;
+    WT *snode = (WT *)smem_raw;  // WORDS node words
     const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
     const int tid = threadIdx.x, NT = blockDim.x;
 
@@ -153,28 +154,34 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     }
     __syncthreads();
 
-    // 1-D max-tree of each row with a stack (pop higher keys; the popped chain
-    // hangs off the next popped element, the last one off the new pixel).
+    // 1-D max-tree of each row with a stack (pop higher keys; the popped chain hangs
+    // off the next popped element, the last one off the new pixel).  The stack is a
+    // list through the parent fields: a pushed pixel links to the element below it,
+    // which is the parent it keeps whether it is popped later (the popped chain) or
+    // stays to the end, so popping only re-links the last popped element.
     const int nrows = TH * TD;
     for (int r = tid; r < nrows; r += NT) {
         int ly = r % TH, lz = r / TH;
         if (ly >= hl || lz >= dl) continue;
-        unsigned short *stk = sstk + r * SS;
-        int sp = 0;
         const int base = r * RS;
+        int top = NONE;
+        WT wtop = 0;
         for (int lx = 0; lx < wl; lx++) {
-            int i = base + lx;
-            uint32_t ki = W::key(snode[i]);
+            const int i = base + lx;
+            const uint32_t ki = W::key(snode[i]);
             int last = NONE;
-            while (sp > 0 && W::key(snode[stk[sp - 1]]) > ki) {
-                int t = stk[--sp];
-                if (last != NONE) snode[last] = W::make(W::key(snode[last]), t);
-                last = t;
+            WT wlast = 0;
+            while (top != NONE && W::key(wtop) > ki) {
+                last = top;
+                wlast = wtop;
+                top = W::par(wtop);
+                if (top != NONE) wtop = snode[top];
             }
-            if (last != NONE) snode[last] = W::make(W::key(snode[last]), i);
-            stk[sp++] = (unsigned short)i;
+            if (last != NONE) snode[last] = W::make(W::key(wlast), i);
+            wtop = W::make(ki, top);
+            snode[i] = wtop;
+            top = i;
         }
-        for (int j = sp - 1; j >= 1; j--) snode[stk[j]] = W::make(W::key(snode[stk[j]]), stk[j - 1]);
     }
     __syncthreads();
 
@@ -227,34 +234,43 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     __syncthreads();
 
     // level-root form inside the tile: pixel -> level root, root -> parent's level
-    // root; to global indices.  Level roots by pointer doubling over the equal-key
-    // links (a flat zone of F pixels can be a chain of ~F links, so walking it from
-    // every pixel would cost O(F^2)): r(i) = parent if it has i's key, else i; then
-    // r(i) = r(r(i)) until every chain (at most WORDS long) has collapsed.
-    unsigned short *sroot = sstk;  // the row stacks (>= WORDS entries) are no longer needed
-    for (int i = tid; i < WORDS; i += NT) {
-        int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
-        unsigned short r = (unsigned short)i;
-        if (lx < wl && ly < hl && lz < dl) {
-            const WT w = snode[i];
-            const int q = W::par(w);
-            if (q != NONE && W::key(snode[q]) == W::key(w)) r = (unsigned short)q;
+    // root; to global indices.  A flat zone of F pixels can be a chain of ~F
+    // equal-key links, so walking it from every pixel would cost O(F^2): instead
+    // every pixel whose parent is not its level root jumps to its grandparent, in
+    // place, round by round.  A word read while its owner rewrites it is the old or
+    // the new link, both equal-key ancestors, so each round at least halves every
+    // distance to a level root as synchronous doubling does: at most
+    // log2(WORDS) + 1 rounds change anything.
+    for (int round = 0;; round++) {
+        int moved = 0;
+        for (int i = tid; i < WORDS; i += NT) {
+            const WT w = acc.load(i);  // padding and outside pixels: no parent
+            const int p = W::par(w);
+            if (p == NONE) continue;
+            const WT wp = acc.load(p);
+            if (W::key(wp) != W::key(w)) continue;  // a level root
+            const int pp = W::par(wp);
+            if (pp == NONE || W::key(acc.load(pp)) != W::key(w)) continue;  // p is the level root
+            acc.store(i, W::make(W::key(w), pp));
+            moved = 1;
         }
-        sroot[i] = r;
-    }
-    __syncthreads();
-    for (int span = 1; span < WORDS; span <<= 1) {
-        for (int i = tid; i < WORDS; i += NT) sroot[i] = sroot[sroot[i]];
-        __syncthreads();
+        if (!__syncthreads_or(moved)) break;
+        if (round > 16) {
+            acc.error(DEVERR_WALK_BOUND);
+            break;
+        }
     }
     for (int i = tid; i < WORDS; i += NT) {
         int lx = i % RS, ly = (i / RS) % TH, lz = i / SLICE;
         if (lx >= wl || ly >= hl || lz >= dl) continue;
         const WT w = snode[i];
-        int p = sroot[i];
-        if (p == i) {  // level root: its parent node's level root
-            const int q = W::par(w);
-            p = q == NONE ? NONE : (int)sroot[q];
+        int p = W::par(w);
+        if (p != NONE) {
+            const WT wp = snode[p];
+            if (W::key(wp) != W::key(w)) {  // i is a level root: its parent node's level root
+                const int pp = W::par(wp);
+                if (pp != NONE && W::key(snode[pp]) == W::key(wp)) p = pp;
+            }
         }
         int out = NONE;
         if (p != NONE) {

@@ -89,6 +89,12 @@ const char *dcf_ctx_last_error(const dcf_ctx *ctx);
 const char *dcf_status_string(dcf_status s);
 /* number of device kernel launches issued through this context so far */
 uint64_t dcf_ctx_launch_count(const dcf_ctx *ctx);
+/* The cudaStream_t every call of this context is ordered on (the one given to
+ * dcf_ctx_create, else one the context created, non-blocking).  Device buffers a
+ * call reads must be ready on it, and device outputs are complete only in its
+ * order: a caller producing or consuming them on another stream orders the two
+ * (an event, or cudaStreamWaitEvent). */
+void *dcf_ctx_stream(const dcf_ctx *ctx);
 
 /* Per-kernel timing with CUDA events on the context's stream (0 = off).  Turning
  * it on or off resets the totals; dcf_ctx_profile returns the summed device time

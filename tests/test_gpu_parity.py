@@ -222,6 +222,30 @@ def test_threaded_oracle_filters_agree_with_gpu(ctx, tree):
             assert np.array_equal(t.filter(0, lam, rule), ref), (rule, lam)
 
 
+def test_device_tensors_ordered_against_torch_stream(ctx):
+    # The context runs on its own non-blocking stream.  A device image whose copy is
+    # queued on torch's stream behind ~25 ms of work is read only after the copy, and
+    # a device output consumed on torch's stream right away is read only after the
+    # filter wrote it (the context's stream held back the same way).
+    torch = pytest.importorskip("torch")
+    if not hasattr(torch.cuda, "_sleep"):
+        pytest.skip("torch.cuda._sleep unavailable")
+    img = smooth_u16(np.random.default_rng(9), 512).astype(np.float32)
+    want_t = gpu_tree(ctx, img, 8)
+    want = want_t.filter(0, 100.0)
+    host = torch.from_numpy(img).pin_memory()
+    d = torch.full(img.shape, -1.0, device="cuda")
+    torch.cuda._sleep(50_000_000)
+    d.copy_(host, non_blocking=True)
+    t = gpu_tree(ctx, d, 8)
+    assert np.array_equal(t.parent(), want_t.parent())
+    out = torch.full(img.shape, -1.0, device="cuda")
+    with torch.cuda.stream(torch.cuda.ExternalStream(ctx.lib.dcf_ctx_stream(ctx.h))):
+        torch.cuda._sleep(50_000_000)
+    t.filter(0, 100.0, out=out)
+    assert np.array_equal(out.cpu().numpy(), want)
+
+
 @pytest.mark.parametrize("kind,conn,tree", [("u8", 4, "max"), ("u16", 8, "min"), ("u16", 8, "max")])
 def test_filter_in_input_type_and_staged_builds(ctx, kind, conn, tree):
     # dcf_filter_as: every rule (and extract) in the input's own integer type equals
