@@ -186,22 +186,62 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
     __syncthreads();
 
     SmemAcc<W> acc{snode, err, WORDS};
-    const Offs offs = forward_offsets(g.conn);
+    const long long bound = merge_bound_smem(g);
     // merge row bands along y (each z slice), then slabs along z; at level k the
-    // seams are the rows (slices) c with c % 2^(k+1) == 2^k
-    for (int axis = 1; axis <= (is3d ? 2 : 1); axis++) {
+    // seams are the rows (slices) c with c % 2^(k+1) == 2^k.  All edges across the
+    // seams of a level at once; correctness does not depend on the order (see
+    // connect).  Levels are ordered for shorter merge walks, not for correctness:
+    // without the barrier warps run ahead into the next level.
+    if (!is3d) {
+        // 2-D (4- or 8-connectivity): pixel p on seam row ly joins q0 above it and,
+        // with 8-connectivity, the diagonals q0 - 1 and q0 + 1 unless implied: a
+        // diagonal p-qd is left out when p's row neighbour toward qd or q0 has a key
+        // >= min(key p, key qd), the rule edge_implied states.  Keys never change, so
+        // each is read once.  Thread t starts at item t (x = t % TW, seam t / TW) and
+        // steps NT items with a carry instead of dividing.
+        const bool diag = g.conn == 8;
+        const int stepx = NT % TW, stepl = NT / TW;
+        for (int half = 1; half < TH; half <<= 1) {
+            const int nseams = (TH + 2 * half - 1) / (2 * half);
+            for (int lx = tid % TW, s = tid / TW; s < nseams;) {
+                const int ly = s * 2 * half + half;
+                if (lx < wl && ly < hl) {
+                    const int p = lx + ly * RS, q0 = p - RS;
+                    connect_s(acc, p, q0, bound);
+                    if (diag) {
+                        const uint32_t kp = W::key(acc.load(p)), k0 = W::key(acc.load(q0));
+                        if (lx > 0) {
+                            const uint32_t kd = W::key(acc.load(q0 - 1)), m = kp < kd ? kp : kd;
+                            if (k0 < m && W::key(acc.load(p - 1)) < m) connect_s(acc, p, q0 - 1, bound);
+                        }
+                        if (lx + 1 < wl) {
+                            const uint32_t kd = W::key(acc.load(q0 + 1)), m = kp < kd ? kp : kd;
+                            if (k0 < m && W::key(acc.load(p + 1)) < m) connect_s(acc, p, q0 + 1, bound);
+                        }
+                    }
+                }
+                lx += stepx;
+                s += stepl;
+                if (lx >= TW) {
+                    lx -= TW;
+                    s++;
+                }
+            }
+            if (g.level_sync) __syncthreads();
+        }
+    }
+    const Offs offs = forward_offsets(g.conn);
+    for (int axis = 1; is3d && axis <= 2; axis++) {
         const int ext = axis == 1 ? TH : TD;
         for (int half = 1; half < ext; half <<= 1) {
             const int nseams = (ext + 2 * half - 1) / (2 * half);
             const int other = axis == 1 ? TD : TH;  // slices (axis y) or rows (axis z)
-            // all edges across the seams of this level at once; correctness does not
-            // depend on the order (see connect)
-            const long long work = (long long)nseams * other * TW;
-            for (long long w = tid; w < work; w += NT) {
-                int lx = (int)(w % TW);
-                long long rest = w / TW;
-                int o = (int)(rest % other);
-                int s = (int)(rest / other);
+            const int work = nseams * other * TW;  // at most 4096 * 26
+            for (int w = tid; w < work; w += NT) {
+                int lx = w % TW;
+                int rest = w / TW;
+                int o = rest % other;
+                int s = rest / other;
                 int c = s * 2 * half + half;  // seam coordinate on the axis
                 int ly, lz;
                 if (axis == 1) { ly = c; lz = o; }
@@ -223,11 +263,9 @@ __device__ __forceinline__ void build_tile(const T *__restrict__ img, long long 
                         };
                         if (edge_implied(-dx, -dy, -dz, kp < kq ? kp : kq, key_at)) continue;
                     }
-                    connect_s(acc, p, qi, merge_bound_smem(g));
+                    connect_s(acc, p, qi, bound);
                 }
             }
-            // levels are ordered for shorter merge walks, not for correctness:
-            // without the barrier warps run ahead into the next level
             if (g.level_sync) __syncthreads();
         }
     }
