@@ -285,20 +285,44 @@ void launch_seam_buckets(SeamEdges &e, unsigned long long *node, long long n, lo
 // canonical form: read-only walks on the node words, each pixel writes only its
 // own parent entry and root flag
 // ---------------------------------------------------------------------------
-__global__ void k_canon(unsigned long long *gnode, Geom g, int *parent, unsigned char *isroot, unsigned *err)
+// The node words are final here (no kernel writes them any more), so they are read
+// through the non-coherent path and stay in L1: a pixel's parent is mostly in its
+// own tile.  Each walk carries the word it loaded last, so a pixel costs its own
+// word, its parent's, and the word that shows where the parent's level ends.
+__global__ void k_canon(const unsigned long long *__restrict__ gnode, Geom g, int *parent, unsigned char *isroot,
+                        unsigned *err)
 {
-    GlobalAcc acc{gnode, err, g.N};
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N;
          p += (long long)gridDim.x * blockDim.x) {
-        const int r = levelroot_ro(acc, (int)p);
+        uint64_t w = __ldg(gnode + p);
+        const uint32_t k = wkey(w);
+        int r = (int)p, q = wpar(w);
+        uint64_t wq = 0;
+        long long it = 0;
+        for (; q != NONE && it <= g.N; it++) {  // p's level root r; q its parent
+            wq = __ldg(gnode + q);
+            if (wkey(wq) != k) break;
+            r = q;
+            q = wpar(wq);
+        }
         if (r != (int)p) {
             parent[p] = r;
             isroot[p] = 0;
         } else {
-            const int q = wpar(acc.load((int)p));
-            parent[p] = q == NONE ? NONE : levelroot_ro(acc, q);
+            int s = q;  // p is a level root: its parent's level root
+            if (q != NONE) {
+                const uint32_t kq = wkey(wq);
+                for (int t = wpar(wq); t != NONE && it <= g.N; it++) {
+                    const uint64_t wt = __ldg(gnode + t);
+                    if (wkey(wt) != kq) break;
+                    s = t;
+                    t = wpar(wt);
+                }
+            }
+            parent[p] = s;
             isroot[p] = 1;
         }
+        if (it > g.N) raise_error(err, DEVERR_WALK_BOUND);
     }
 }
 

@@ -164,27 +164,6 @@ __device__ __forceinline__ uint64_t wmake(uint32_t key, int par)
     return ((uint64_t)key << 32) | (uint32_t)(par == NONE ? 0xFFFFFFFFu : (uint32_t)par);
 }
 
-// Read-only level-root walk for the final canonicalisation passes: there every
-// thread writes only its own entry, because a path-halving write from another
-// thread could land after a fully compressed one and undo it.
-template <class A>
-__device__ __forceinline__ int levelroot_ro(A &acc, int i)
-{
-    uint64_t w = acc.load(i);
-    const uint32_t k = wkey(w);
-    const long long bound = acc.walk_bound();
-    for (long long it = 0; it < bound; it++) {
-        const int p = wpar(w);
-        if (p == NONE) return i;
-        const uint64_t wp = acc.load(p);
-        if (wkey(wp) != k) return i;
-        i = p;
-        w = wp;
-    }
-    acc.error(DEVERR_WALK_BOUND);
-    return i;
-}
-
 // Level root of i given its word w, continuing past equal-key links (with path
 // halving); on return (i, w) is the level root and (ni, nw) the first pixel of
 // the parent node and its word (ni = NONE at a root).  The parent's word is the
