@@ -457,12 +457,12 @@ static void attr_carve(AttrBufs &a, int group, bool exact_g, bool has_z, size_t 
     a.single = (unsigned char *)m;
 }
 
-// zero every record, bounding-box minima to all-ones, 2-D z extent to [0, 1)
-static cudaError_t attr_zero(const AttrBufs &a, size_t N, void *mem, int sm, cudaStream_t s)
+// start values of the level roots' records (the only records any pass reads)
+static cudaError_t attr_zero(const AttrBufs &a, const int *nodes, const unsigned long long *num_nodes, size_t N,
+                             int sm, cudaStream_t s)
 {
-    cudaError_t e = cudaMemsetAsync(mem, 0, attr_bytes(a.group, N) - 256, s);
-    if (e == cudaSuccess && a.group == 1) launch_attr_init(a, (long long)N, sm, s);
-    return e;
+    launch_attr_init(a, NodeSet{nodes, num_nodes}, (long long)N, sm, s);
+    return cudaGetLastError();
 }
 
 // allocate and accumulate the records of attr_idx's group
@@ -481,7 +481,7 @@ static dcf_status compute_attributes(dcf_ctx *ctx, dcf_tree *t, int attr_idx, bo
     AttrBufs &a = t->attr;
     attr_carve(a, group, t->dtype == U8 || t->dtype == U16, t->g.D > 1, N, t->attr_mem);
     if (need_grey) a.grey = true;
-    CU(attr_zero(a, N, t->attr_mem, ctx->sm_count, ctx->stream));
+    CU(attr_zero(a, t->nodes, t->num_nodes, N, ctx->sm_count, ctx->stream));
     unsigned *count = ctx->d_err + 2;
     launch_attributes(view_of(t), a, count, ctx->up_steps, ctx->d_err, ctx->sm_count, ctx->stream);
     dcf_status st = check_launch(ctx, 4);
@@ -1350,7 +1350,7 @@ static dcf_status batch_forward(dcf_ctx *ctx, dcf_batch *b, const void *px, floa
     launch_stats(b->dtype, px, b->N, b->d_misc + 2, b->d_misc + 3, b->d_misc + 4, sm, s);
     launch_batch_build(b->dtype, px, v.g, b->d_imgs, b->d_tiles, b->ntiles, b->chunk, b->d_misc, b->gval, b->node,
                        b->parent, b->isroot, b->d_nodes, b->nodes, ctx->d_err, b->ctas, b->seam, sm, s);
-    CU(attr_zero(b->attr, (size_t)b->N, b->attr_mem, sm, s));
+    CU(attr_zero(b->attr, b->nodes, b->d_nodes, (size_t)b->N, sm, s));
     launch_batch_attr_pixels(v.g, b->d_imgs, b->d_tiles, b->ntiles, b->gval, b->parent, b->isroot, b->attr, sm, s);
     unsigned *count = b->d_misc + 1;
     launch_attributes_up(v, b->attr, count, b->up_steps, ctx->d_err, sm, s);

@@ -246,23 +246,35 @@ void launch_fill_u32(long long n, uint32_t *dst, uint32_t v, int sm, cudaStream_
     k_fill_u32<<<grid_for(n, 256, sm), 256, 0, s>>>(n, dst, v); note_launch();
 }
 
-// start values of the extent group's interleaved records (two 16-byte stores each):
-// area and pending 0, bounding-box minima all-ones, maxima 0; in 2-D every pixel has
-// z = 0, so the z extent is the fixed [0, 1)
-__global__ void k_attr_init_extent(long long n, uint4 *rec, bool has_z)
+// Start values of the level roots' records.  The extent group's interleaved record
+// is two 16-byte stores: area and pending 0, bounding-box minima all-ones, maxima 0;
+// in 2-D every pixel has z = 0, so the z extent is the fixed [0, 1).  The other
+// groups' area/pending pair is one 8-byte store, then their 64-bit sums.
+__global__ void k_attr_init(NodeSet ns, AttrBufs a)
 {
     const uint4 lo = make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
-    const uint4 hi = has_z ? make_uint4(0xFFFFFFFFu, 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, 1u);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        rec[2 * i] = lo;
-        rec[2 * i + 1] = hi;
+    const uint4 hi = a.has_z ? make_uint4(0xFFFFFFFFu, 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, 1u);
+    NODE_LOOP(u, ns.nodes, ns.num)
+    {
+        if (a.group == 1) {
+            uint4 *rec = (uint4 *)(a.area.p + (size_t)REC1_WORDS * u);
+            rec[0] = lo;
+            rec[1] = hi;
+            continue;
+        }
+        *(uint2 *)(a.area.p + 2 * (size_t)u) = make_uint2(0u, 0u);
+        for (int d = 0; d < 3; d++)
+            if (a.s1[d]) a.s1[d][u] = 0ull;
+        for (int d = 0; d < 6; d++)
+            if (a.s2[d]) a.s2[d][u] = 0ull;
+        for (int d = 0; d < 5; d++)
+            if (a.gw[d]) ((unsigned long long *)a.gw[d])[u] = 0ull;
     }
 }
 
-void launch_attr_init(const AttrBufs &a, long long n, int sm, cudaStream_t s)
+void launch_attr_init(const AttrBufs &a, NodeSet ns, long long n, int sm, cudaStream_t s)
 {
-    if (a.group != 1) return;  // the other groups start at zero (the caller's memset)
-    k_attr_init_extent<<<grid_for(n, 256, sm), 256, 0, s>>>(n, (uint4 *)a.area.p, a.has_z); note_launch();
+    k_attr_init<<<grid_for(n, 256, sm), 256, 0, s>>>(ns, a); note_launch();
 }
 
 // leaves get pending = -1; nodes with exactly one child are flagged in `single`

@@ -179,9 +179,12 @@ struct AttrBufs {
     bool grey = true;                // inertia group: accumulate the grey-weighted sums too
 };
 
-// every record of `a` over n pixels set to its start value: zero sums, empty
-// bounding boxes (minimum all-ones), and in 2-D the fixed z extent [0, 1)
-void launch_attr_init(const AttrBufs &a, long long n, int sm_count, cudaStream_t s);
+// the record of every level root in `ns` set to its start value: zero area, pending
+// and sums, empty bounding boxes (minimum all-ones), in 2-D the fixed z extent
+// [0, 1).  Only level roots' records are ever read or written (pixels add into
+// their node's), so the other pixels' records are left as they are; n bounds the
+// node count (grid size)
+void launch_attr_init(const AttrBufs &a, NodeSet ns, long long n, int sm_count, cudaStream_t s);
 
 // Fields a pass must move: z moments only in 3-D; grey-weighted sums for the wmean
 // group, and for the inertia group only when asked (its attributes 13-17 use the
