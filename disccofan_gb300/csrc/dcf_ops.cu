@@ -2,9 +2,11 @@
 // per-pixel parts of operation.c), re-designed as node-parallel passes:
 //
 //   k_flag          survive bit of every level root: attribute >= lambda.
-//   k_resolve       each node finds its nearest flagged ancestor-or-self by walking
-//                   up; results are written back along the walked path so later
-//                   walkers stop early (direct and max rules, filtering.c:102,156).
+//   k_resolve_halving  direct rule (filtering.c:102-154): each node finds its
+//                   nearest surviving ancestor-or-self by path halving.
+//   k_resolve       max rule (filtering.c:156): nearest kept ancestor-or-self by
+//                   walking up; results are written back along the walked path so
+//                   later walkers stop early.
 //   k_mark_kept     max rule: every survivor marks its ancestors as kept.
 //   k_jump_*        pointer jumping over root paths with double buffers: path sums
 //                   for the subtractive rule (filtering.c:211-261) and the topmost
@@ -28,16 +30,16 @@ constexpr int UNKNOWN = -2;
 #define GRID_LOOP(p, n) \
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < (n); p += (long long)gridDim.x * blockDim.x)
 
-// presolve (direct rule): a surviving node is its own resolution, so k_resolve<.., true>
-// walks on `target` alone
-__global__ void k_flag(Geom g, NodeSet ns, AttrBufs a, int attr, double lambda,
-                       float pd0, float pd1, float pd2, unsigned char *flag, int *target, bool presolve)
+// presolve (direct rule): target starts as the forest k_resolve_halving searches, a
+// surviving node pointing to itself and any other node to its parent
+__global__ void k_flag(Geom g, NodeSet ns, AttrBufs a, int attr, double lambda, float pd0, float pd1, float pd2,
+                       const int *__restrict__ parent, unsigned char *flag, int *target, bool presolve)
 {
     const float pd[3] = {pd0, pd1, pd2};
     NODE_LOOP(p, ns.nodes, ns.num)
     {
         const bool keep = attr_value(a, attr, (int)p, pd) >= lambda;
-        target[p] = presolve && keep ? p : UNKNOWN;
+        target[p] = !presolve ? UNKNOWN : keep ? p : parent[p];
         flag[p] = keep ? 1 : 0;
     }
 }
@@ -59,8 +61,7 @@ __global__ void k_mark_kept(Geom g, NodeSet ns, const int *__restrict__ parent,
 }
 
 // nearest flagged ancestor-or-self; flag may be a byte array or the kept words
-// (PRESOLVED: the flagged nodes already hold themselves in target; flag unused)
-template <typename F, bool PRESOLVED>
+template <typename F>
 __global__ void k_resolve(Geom g, NodeSet ns, const int *__restrict__ parent,
                           const F *__restrict__ flag, int *target, unsigned *err)
 {
@@ -72,7 +73,7 @@ __global__ void k_resolve(Geom g, NodeSet ns, const int *__restrict__ parent,
         for (; it < g.N; it++) {
             int t = ((volatile int *)target)[v];
             if (t != UNKNOWN) { res = t; break; }
-            if (!PRESOLVED && flag[v]) { res = v; break; }
+            if (flag[v]) { res = v; break; }
             int q = parent[v];
             if (q == NONE) { res = NONE; break; }
             v = q;
@@ -80,6 +81,44 @@ __global__ void k_resolve(Geom g, NodeSet ns, const int *__restrict__ parent,
         if (it >= g.N) raise_error(err, DEVERR_WALK_BOUND);
         for (int w = (int)p; w != v; w = parent[w]) ((volatile int *)target)[w] = res;
         ((volatile int *)target)[v] = res;
+    }
+}
+
+// Direct rule: nearest surviving ancestor-or-self, by path halving on the forest
+// k_flag left in target (survivors point to themselves, other nodes to their
+// parent; NONE above an unflagged root).  A walk that ends only after its result is
+// known leaves nothing for the nodes it passed, so the nodes of one unflagged chain,
+// which sit together in the node list and start together, would each walk the whole
+// chain; halving shares every step at once.  Every pointer stays an ancestor at or
+// below the nearest survivor, and each node's own thread writes its answer last: a
+// halving CAS expects the pointer it read, so a late one cannot replace an answer.
+__global__ void k_resolve_halving(Geom g, NodeSet ns, int *target, unsigned *err)
+{
+    volatile int *tg = target;
+    NODE_LOOP(p, ns.nodes, ns.num)
+    {
+        int v = (int)p, j = tg[v];
+        if (j == v) continue;  // survives: its own resolution
+        int res = NONE;
+        long long it = 0;
+        for (; it < g.N; it++) {
+            if (j == NONE) break;  // above an unflagged root
+            const int jj = tg[j];
+            if (jj == j) {  // j survives
+                res = j;
+                break;
+            }
+            if (jj == NONE) break;
+            atomicCAS(target + v, j, jj);
+            v = jj;
+            j = tg[v];
+            if (j == v) {
+                res = v;
+                break;
+            }
+        }
+        if (it >= g.N) raise_error(err, DEVERR_WALK_BOUND);
+        tg[p] = res;
     }
 }
 
@@ -247,17 +286,17 @@ void launch_filter(const TreeView &t, const AttrBufs &a, int attr, int rule, dou
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
-    k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
-                              w.target, rule == 0); note_launch();
+    k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2],
+                              t.parent, w.flag, w.target, rule == 0); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(rule == 0 || rule == 2 ? P_RESOLVE : P_JUMP, s);
     const double *accp = nullptr;
     if (rule == 0) {
-        k_resolve<unsigned char, true><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
+        k_resolve_halving<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, w.target, err); note_launch();
     } else if (rule == 2) {
         cudaMemsetAsync(w.kept, 0, t.g.N * sizeof(unsigned), s);
         k_mark_kept<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.kept, err); note_launch();
-        k_resolve<unsigned, false><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.kept, w.target, err); note_launch();
+        k_resolve<unsigned><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.kept, w.target, err); note_launch();
     } else {
         const int R = rounds_for(depth_bound);
         int *j0 = w.jump, *j1 = w.jump2;
@@ -820,11 +859,11 @@ void launch_direct_targets(const TreeView &t, const AttrBufs &a, int attr, doubl
 {
     const int nb = grid_for(t.g.N, 256, sm);
     prof_begin(P_FLAG, s);
-    k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2], w.flag,
-                              w.target, true); note_launch();
+    k_flag<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, a, attr, lambda, t.pixdim[0], t.pixdim[1], t.pixdim[2],
+                              t.parent, w.flag, w.target, true); note_launch();
     prof_end(P_FLAG, s);
     prof_begin(P_RESOLVE, s);
-    k_resolve<unsigned char, true><<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, t.parent, w.flag, w.target, err); note_launch();
+    k_resolve_halving<<<nb, 256, 0, s>>>(t.g, NodeSet{t.nodes, t.num_nodes}, w.target, err); note_launch();
     prof_end(P_RESOLVE, s);
 }
 
