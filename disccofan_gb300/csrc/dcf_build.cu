@@ -5,14 +5,17 @@
 //   k_stats        min / max / NaN scan of the input (preprocessing.c:7-30).
 //   k_tile_build   one CTA builds the max-tree of one tile in shared memory: a 1-D
 //                  stack pass per row, then the rows are merged band by band with the
-//                  lock-free connect() on 64-bit shared-memory node words; the tile's
-//                  forest goes to the HBM node array in level-root form.
-//   k_seam_merge   every edge that crosses a tile boundary is merged with connect()
+//                  lock-free connect() on shared-memory node words (32-bit for u8/u16,
+//                  64-bit for u32/f32); the tile's forest goes to the HBM node array
+//                  in level-root form (dcf_tile.cuh).
+//   k_seam_collect, k_seam_bucket (or k_seam_direct)
+//                  every edge that crosses a tile boundary is merged with connect()
 //                  on the HBM node array (64-bit CAS): the on-device replacement of
 //                  the MPI boundary-tree exchange and merge.
 //   k_canon        flatten to the reference's canonical form (flood.c:127-141,
 //                  get_levelroot :693-712) into the int32 parent array: pixel ->
-//                  level root, root -> parent's level root; root flags; node count.
+//                  level root, root -> parent's level root; root flags.  Then the
+//                  level-root list (k_nodes_count/scan/emit).
 #include "dcf_tile.cuh"
 
 namespace dcf {
