@@ -247,8 +247,19 @@ def run_ours(args):
         barrier()
         ev0.record(stream)
         streams[1].wait_event(ev0)
-        for _ in range(args.steps):
-            step()
+        if concurrent:
+            # each tree's thread runs its K steps back to back, with no join between
+            # steps: the two trees drift out of phase, so one's latency-bound phases
+            # (seam zips, walks) overlap the other's issue-bound tile build
+            def tree_steps(k):
+                for _ in range(args.steps):
+                    t = tree_work(k, ctxs[k], img)
+                    t.close()
+            for f in [pool.submit(tree_steps, k) for k in range(2)]:
+                f.result()
+        else:
+            for _ in range(args.steps):
+                step()
         stream.wait_stream(streams[1])
         ev1.record(stream)
         barrier()
@@ -370,7 +381,8 @@ def run_ours(args):
                                          "traffic_ratio": None if pipeline_traffic is None else
                                          round(pipeline_traffic / B_alg, 3),
                                          "dram_source": dram["source"] if dram else None},
-                   "trees": "concurrent (two contexts, two streams)" if concurrent else "serial (one stream)",
+                   "trees": ("concurrent (two contexts, two streams; each tree's K steps back to back on its own "
+                             "host thread)") if concurrent else "serial (one stream)",
                    "kernel_ms_per_step": {k: round(v[0] / prof_steps, 3) for k, v in sorted(prof.items())},
                    "kernel_split": f"CUDA events on one stream over {prof_steps} serial steps "
                                    f"({prof_ms_step:.1f} ms/step of kernels)"},
