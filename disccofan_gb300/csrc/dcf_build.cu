@@ -91,17 +91,20 @@ __device__ __forceinline__ bool seam_item(const Geom &g, int ntx, int nty, const
                                           const unsigned long long *gnode, int &p, int &q)
 {
     const int TW = g.tw, TH = g.th, TD = g.td;
-    const int e = (int)(w % offs.n);
-    long long r = w / offs.n;
-    const int k = (int)(r % fmax);
-    r /= fmax;
-    const int f = (int)(r % 5);
-    const long long tile = r / 5;
+    // w = ((tile * 5 + f) * fmax + k) * offs.n + e: one 64-bit division splits off
+    // the tile, the rest (below 5 * 4096 * 13) is decoded in 32 bits
+    const int span = 5 * fmax * offs.n;
+    const int tile = (int)(w / span);
+    int r = (int)(w - (long long)tile * span);
+    const int e = r % offs.n;
+    r /= offs.n;
+    const int k = r % fmax;
+    const int f = r / fmax;
     const int dx = offs.d[e][0], dy = offs.d[e][1], dz = offs.d[e][2];
     const bool out = f == 0 ? dx > 0 : f == 1 ? dx < 0 : f == 2 ? dy > 0 : f == 3 ? dy < 0 : dz > 0;
     const int fpix = f <= 1 ? TH * TD : (f <= 3 ? TW * TD : TW * TH);
     if (!out || k >= fpix || (f == 4 && g.D == 1)) return false;
-    const int tx = (int)(tile % ntx), ty = (int)((tile / ntx) % nty), tz = (int)(tile / ((long long)ntx * nty));
+    const int tx = tile % ntx, ty = (tile / ntx) % nty, tz = tile / (ntx * nty);
     const int x0 = tx * TW, y0 = ty * TH, z0 = tz * TD;
     const int wl = min(TW, g.W - x0), hl = min(TH, g.H - y0), dl = min(TD, g.D - z0);
     int lx, ly, lz;
