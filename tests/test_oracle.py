@@ -91,6 +91,26 @@ def test_port_threads_agree_after_canonicalisation(port_lib, synthetic):
     assert np.array_equal(four.pattern(0, [5, 20, 100]), one.pattern(0, [5, 20, 100]))
 
 
+@pytest.mark.parametrize("tree", ["max", "min"])
+def test_port_threaded_filters_agree_across_slab_seams(port_lib, tree):
+    # The filter threads stop at nodes other threads resolved and copy their value;
+    # on smooth images whose level components cross every slab seam the threaded
+    # rules 0, 1 and 3 must equal the single-threaded ones (the copy is published
+    # with release/acquire ordering, which weakly ordered hosts need)
+    rng = np.random.default_rng(11)
+    n = 384
+    f = np.fft.rfft2(rng.standard_normal((n, n)))
+    k2 = np.fft.fftfreq(n)[:, None] ** 2 + np.fft.rfftfreq(n)[None, :] ** 2
+    s = np.fft.irfft2(f * np.exp(-k2 * (n / 24.0) ** 2), (n, n))
+    img = ((s - s.min()) / (s.max() - s.min()) * 40000).astype(np.uint16).astype(np.float32)
+    one, many = port_lib.Port(threads=1), port_lib.Port(threads=8)
+    one.load(img, 8, tree, threads=1)
+    many.load(img, 8, tree, threads=8)
+    for rule in (0, 1, 3):
+        for lam in (50.0, 2000.0):
+            assert np.array_equal(many.filter(0, lam, rule), one.filter(0, lam, rule)), (rule, lam)
+
+
 def test_eigen_restatement_diagonal_exact(port_lib):
     import ctypes as C
     p = port_lib.Port()
