@@ -416,6 +416,48 @@ __global__ void k_attr_up(const int *__restrict__ nodes, const unsigned long lon
         int u = p;
         Rec<G, EXACT> r;
         rec_load<G, EXACT>(a, u, r);
+        if constexpr (G == 1) {
+            // The extent record is one 32-byte sector, so each step reads everything it
+            // may need at the parent q at once -- the single-child flag, q's record and
+            // q's own parent (the next step's q) -- instead of one after the other: a
+            // single-child step, the common one along chains, costs one round trip.
+            // Only this walker writes a single-child parent; a parent with more
+            // children takes the atomics below and ignores the record read early.
+            int q = parent[u];
+            for (int step = 0; q != NONE; step++) {
+                if (step == up_steps) {
+                    a.pending[u] = STALLED;
+                    break;
+                }
+                const unsigned char sq = a.single[q];
+                uint4 *rp = (uint4 *)(a.area + q);
+                const uint4 q0 = __ldcg(rp), q1 = __ldcg(rp + 1);
+                const int qq = parent[q];
+                if (sq) {
+                    r.area += q0.x;
+                    r.bmin[0] = min(r.bmin[0], q0.z);
+                    r.bmin[1] = min(r.bmin[1], q0.w);
+                    r.bmin[2] = min(r.bmin[2], q1.x);
+                    r.bmax[0] = max(r.bmax[0], q1.y);
+                    r.bmax[1] = max(r.bmax[1], q1.z);
+                    r.bmax[2] = max(r.bmax[2], q1.w);
+                    __stcg(rp, make_uint4(r.area, 0u, r.bmin[0], r.bmin[1]));  // pending cleared
+                    __stcg(rp + 1, make_uint4(r.bmin[2], r.bmax[0], r.bmax[1], r.bmax[2]));
+                    u = q;
+                    q = qq;
+                    continue;
+                }
+                rec_fold<G, EXACT>(a, q, r);
+                __threadfence();
+                const int before = atomicSub(a.pending + q, 1);
+                if (before != 1) break;
+                __threadfence();
+                u = q;
+                q = qq;
+                rec_load<G, EXACT>(a, u, r);
+            }
+            continue;
+        }
         for (int step = 0;; step++) {
             const int q = parent[u];
             if (q == NONE) break;
